@@ -1,0 +1,187 @@
+/*
+ * smearfem_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * smearFEM.jl hot path: Q1/Q2 element stiffness with 2x2(x2) Gauss
+ * quadrature, global sparse assembly, Dirichlet elimination and the solve of
+ * K u = f.
+ *
+ * The entry points are what a Julia `ccall` binding (or Python ctypes, or C)
+ * needs to replace the reference's calling surface:
+ *
+ *   gaussian_quadrature(a,b,nGaussPoints)         src/fem.jl:21-31
+ *   basis_function(xi,eta,zeta,FunctionClass)     src/fem.jl:48-114
+ *   assemble_system(ne,NodeList,IEN,ndim,
+ *                   FunctionClass,nDof,ID,Young,nu) src/fem.jl:135-256
+ *   setboundaryCond / C'*K_bar*C / inv(Matrix(K_free)) / q_d + C*q_f
+ *                                                  examples/vector3D.jl:133-173,315-322
+ *
+ * Conventions
+ *  - Arrays use the reference's (Julia) layout: column-major, 1-based indices.
+ *      NodeList : double [ndim x nNodes]   (xyz of a node contiguous)
+ *      IEN      : int64  [ldIEN x nen]     (element index fastest)
+ *      ID       : int64  [nNodes x nDof]
+ *    The matrix is returned in SparseMatrixCSC form (colptr, rowval, nzval;
+ *    1-based, rows sorted per column, explicit zeros kept).
+ *  - `mem_space` says where every pointer argument of that call lives:
+ *    SFEM_MEM_HOST (any host memory; copies are staged by the library) or
+ *    SFEM_MEM_DEVICE (device memory of the context's GPU).
+ *  - Every function returns an sfem_status.  sfem_last_error() gives a
+ *    human-readable reason for the last failure on a context.
+ *  - Ownership: handles are created and destroyed by the library.  Output
+ *    arrays are allocated by the caller; sizes come from sfem_matrix_info.
+ *  - A context owns one CUDA stream and is not thread-safe.  Calls are
+ *    synchronous: when they return, outputs are complete.
+ *  - There is no CPU fallback: if no GPU is usable, sfem_ctx_create fails.
+ */
+#ifndef SMEARFEM_GPU_H
+#define SMEARFEM_GPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SFEM_API __attribute__((visibility("default")))
+#else
+#define SFEM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SFEM_OK = 0,
+    SFEM_BAD_ARG = 1,            /* invalid argument (sizes, classes, NULLs)          */
+    SFEM_BAD_INDEX = 2,          /* IEN/ID entry out of range (Julia: BoundsError)    */
+    SFEM_SINGULAR_JACOBIAN = 3,  /* det J == 0 at a Gauss point (Julia: inv throws)   */
+    SFEM_OOM = 4,                /* device allocation failed                          */
+    SFEM_NOT_CONVERGED = 5,      /* maxit reached before rtol                         */
+    SFEM_CUDA_ERROR = 6,         /* CUDA runtime error                                */
+    SFEM_SINGULAR = 7,           /* K_free singular: zero pivot / CG breakdown        */
+    SFEM_UNSUPPORTED = 8         /* element class the reference cannot assemble       */
+} sfem_status;
+
+enum { SFEM_MEM_HOST = 0, SFEM_MEM_DEVICE = 1 };
+enum { SFEM_Q1 = 1, SFEM_Q2 = 2 };                      /* FunctionClass              */
+enum { SFEM_PLANE_STRESS = 0, SFEM_PLANE_STRAIN = 1 };  /* 2D elasticity law          */
+enum { SFEM_FP64 = 0, SFEM_MIXED = 1 };                 /* solver precision           */
+enum { SFEM_PC_JACOBI = 0, SFEM_PC_BLOCK_JACOBI = 1 };  /* preconditioner             */
+
+typedef struct sfem_ctx sfem_ctx;
+typedef struct sfem_mesh sfem_mesh;
+typedef struct sfem_matrix sfem_matrix;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Create a context on CUDA device `device` (no reference counterpart: the
+ * reference runs in one Julia thread on the CPU). */
+SFEM_API int sfem_ctx_create(int device, sfem_ctx **out);
+SFEM_API int sfem_ctx_destroy(sfem_ctx *ctx);
+SFEM_API const char *sfem_last_error(const sfem_ctx *ctx);
+/* Wait for all work on the context's stream. */
+SFEM_API int sfem_ctx_synchronize(sfem_ctx *ctx);
+/* Library version string. */
+SFEM_API const char *sfem_version(void);
+
+/* ---- host helpers (pure host code, identical expressions) --------------- */
+
+/* gaussian_quadrature(a,b,nGaussPoints), src/fem.jl:21-31.
+ * xi, w: caller arrays of length nGaussPoints (2 or 3). */
+SFEM_API int sfem_gaussian_quadrature(double a, double b, int nGaussPoints, double *xi, double *w);
+
+/* basis_function(xi,eta,zeta,FunctionClass), src/fem.jl:48-114.
+ * ndim 1..3 (Q1) or 2 (Q2).  N: nen values; dN: nen x ndim column-major
+ * (column k = dN/dxi_k), exactly the reference's hcat layout. */
+SFEM_API int sfem_basis_function(int ndim, int function_class, double xi, double eta, double zeta,
+                        double *N, double *dN);
+
+/* ---- mesh and sparsity pattern ------------------------------------------ */
+
+/* Upload and validate a mesh: the inputs of assemble_system
+ * (src/fem.jl:135, with ne^ndim elements processed, src/fem.jl:179).
+ *   ne        elements per direction; the first ne^ndim rows of IEN are used
+ *   nen       columns of IEN: 2^ndim for Q1, 9 for Q2
+ *   nDof      1 (scalar Laplace) or ndim (elasticity); ID may be NULL if 1
+ * IEN entries must lie in 1..nNodes and ID entries of referenced nodes must
+ * be >= 1 and distinct (SFEM_BAD_INDEX / SFEM_BAD_ARG otherwise). */
+SFEM_API int sfem_mesh_create(sfem_ctx *ctx, int ndim, int function_class, int nDof, int64_t ne,
+                     const double *NodeList, int64_t nNodes, const int64_t *IEN,
+                     int64_t ldIEN, int nen, const int64_t *ID, int mem_space,
+                     sfem_mesh **out);
+SFEM_API int sfem_mesh_destroy(sfem_mesh *mesh);
+
+/* Build the sparsity pattern of K on the device: the structure that
+ * sparse(E,J,V) produces at src/fem.jl:253 (union of element DOF-pair
+ * blocks, explicit zeros kept).  n_out = size(K,1) = maximum row index,
+ * nnz_out = nnz(K).  Idempotent; assembly builds it on demand. */
+SFEM_API int sfem_pattern_build(sfem_ctx *ctx, sfem_mesh *mesh, int64_t *n_out, int64_t *nnz_out);
+
+/* ---- assembly ----------------------------------------------------------- */
+
+/* Numeric assembly of K on a mesh (src/fem.jl:179-252): per element the
+ * Jacobian, |det J|-weighted Gauss sum of B'DB (or grad N_i . grad N_j),
+ * summed into the pattern in ascending element order without atomics.
+ * Young/nu: length 1 (the reference's scalars) or ne^ndim (per element).
+ * plane selects the 2D law (the reference's is plane stress). */
+SFEM_API int sfem_assemble(sfem_ctx *ctx, sfem_mesh *mesh, int plane, const double *Young,
+                  int64_t nYoung, const double *nu, int64_t nNu, int mem_space,
+                  sfem_matrix **out);
+
+/* One call doing mesh upload + pattern + assembly: assemble_system(ne,
+ * NodeList, IEN, ndim, FunctionClass, nDof, ID, Young, nu), src/fem.jl:135.
+ * The returned matrix keeps the mesh it was built on alive. */
+SFEM_API int sfem_assemble_system(sfem_ctx *ctx, int64_t ne, const double *NodeList, int64_t nNodes,
+                         const int64_t *IEN, int64_t ldIEN, int nen, int ndim,
+                         int function_class, int nDof, const int64_t *ID, const double *Young,
+                         int64_t nYoung, const double *nu, int64_t nNu, int plane,
+                         int mem_space, sfem_matrix **out, int64_t *n_out, int64_t *nnz_out);
+
+/* n = size(K,1) = size(K,2); nnz = length(nzval). */
+SFEM_API int sfem_matrix_info(const sfem_matrix *K, int64_t *n, int64_t *nnz);
+
+/* Copy K out in SparseMatrixCSC form (the return value of assemble_system,
+ * src/fem.jl:253-255).  colptr: n+1, rowval: nnz, nzval: nnz; any may be
+ * NULL to skip it.  1-based indices. */
+SFEM_API int sfem_matrix_export_csc(sfem_ctx *ctx, const sfem_matrix *K, int64_t *colptr,
+                           int64_t *rowval, double *nzval, int mem_space);
+SFEM_API int sfem_matrix_destroy(sfem_matrix *K);
+
+/* ---- Dirichlet elimination and solve ------------------------------------ */
+
+typedef struct {
+    int precision;        /* SFEM_FP64 (default) or SFEM_MIXED                    */
+    int precond;          /* SFEM_PC_JACOBI (default) or SFEM_PC_BLOCK_JACOBI     */
+    double rtol;          /* stop at ||f_f - K_ff u_f|| <= rtol ||f_f - K_fd u_d|| */
+    int maxit;            /* iteration cap (SFEM_NOT_CONVERGED beyond it)          */
+    int check_every;      /* iterations per device-side chunk between host checks */
+    double reliable_delta;/* mixed: refresh the FP64 residual when the FP32
+                             residual has dropped by this factor                 */
+    int profile;          /* 1: time the SpMV launches with CUDA events           */
+} sfem_solve_opts;
+
+typedef struct {
+    int status;           /* sfem_status of the solve                              */
+    int iterations;       /* CG iterations (inner iterations for SFEM_MIXED)       */
+    int reliable_updates; /* FP64 residual refreshes (SFEM_MIXED)                  */
+    double relres;        /* final relative residual (FP64 true residual)          */
+    double ms_total;      /* wall time of the solve call                           */
+    double ms_spmv;       /* summed CUDA-event time of the SpMV launches (profile) */
+    int spmv_launches;    /* SpMV launches timed                                   */
+    int kernel_launches;  /* kernels launched by the solve                         */
+    int64_t n_free;       /* free DOFs                                             */
+} sfem_solve_stats;
+
+SFEM_API void sfem_solve_opts_default(sfem_solve_opts *opts);
+
+/* Solve K u = f with u prescribed on `fixed_dofs` (1-based global DOF ids,
+ * values `fixed_vals`): the elimination of examples/vector3D.jl:314-322,
+ *   K_free = C'KC;  q_f = K_free \ C'(f - K q_d);  u = q_d + C q_f,
+ * with the reference's dense inverse replaced by preconditioned CG on the
+ * GPU.  f may be NULL (the reference's case, f = 0).  u_out has n entries. */
+SFEM_API int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t *fixed_dofs,
+                         int64_t nfix, const double *fixed_vals, const double *f,
+                         double *u_out, int mem_space, const sfem_solve_opts *opts,
+                         sfem_solve_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMEARFEM_GPU_H */

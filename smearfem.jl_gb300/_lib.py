@@ -1,0 +1,101 @@
+"""ctypes binding of libsmearfem_gpu.so (include/smearfem_gpu.h).
+
+The library is the product: there is no CPU fallback.  If the shared object
+is missing, :func:`lib` raises with the build command; if no GPU is usable,
+``sfem_ctx_create`` fails and :class:`SfemError` is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libsmearfem_gpu.so")
+
+SFEM_OK, SFEM_BAD_ARG, SFEM_BAD_INDEX, SFEM_SINGULAR_JACOBIAN, SFEM_OOM = 0, 1, 2, 3, 4
+SFEM_NOT_CONVERGED, SFEM_CUDA_ERROR, SFEM_SINGULAR, SFEM_UNSUPPORTED = 5, 6, 7, 8
+STATUS_NAMES = {0: "SFEM_OK", 1: "SFEM_BAD_ARG", 2: "SFEM_BAD_INDEX", 3: "SFEM_SINGULAR_JACOBIAN",
+                4: "SFEM_OOM", 5: "SFEM_NOT_CONVERGED", 6: "SFEM_CUDA_ERROR", 7: "SFEM_SINGULAR",
+                8: "SFEM_UNSUPPORTED"}
+MEM_HOST, MEM_DEVICE = 0, 1
+Q1, Q2 = 1, 2
+PLANE_STRESS, PLANE_STRAIN = 0, 1
+FP64, MIXED = 0, 1
+PC_JACOBI, PC_BLOCK_JACOBI = 0, 1
+
+
+class SfemError(RuntimeError):
+    """A non-OK sfem_status; ``code`` holds the status value."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("precond", C.c_int), ("rtol", C.c_double),
+                ("maxit", C.c_int), ("check_every", C.c_int), ("reliable_delta", C.c_double),
+                ("profile", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("reliable_updates", C.c_int),
+                ("relres", C.c_double), ("ms_total", C.c_double), ("ms_spmv", C.c_double),
+                ("spmv_launches", C.c_int), ("kernel_launches", C.c_int), ("n_free", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+P = C.c_void_p
+PP = C.POINTER(C.c_void_p)
+I64 = C.c_int64
+I64P = C.POINTER(C.c_int64)
+
+# name: (restype, argtypes) -- mirrors include/smearfem_gpu.h
+SIGNATURES = {
+    "sfem_ctx_create": (C.c_int, [C.c_int, PP]),
+    "sfem_ctx_destroy": (C.c_int, [P]),
+    "sfem_last_error": (C.c_char_p, [P]),
+    "sfem_ctx_synchronize": (C.c_int, [P]),
+    "sfem_version": (C.c_char_p, []),
+    "sfem_gaussian_quadrature": (C.c_int, [C.c_double, C.c_double, C.c_int, P, P]),
+    "sfem_basis_function": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, P, P]),
+    "sfem_mesh_create": (C.c_int, [P, C.c_int, C.c_int, C.c_int, I64, P, I64, P, I64, C.c_int, P,
+                                   C.c_int, PP]),
+    "sfem_mesh_destroy": (C.c_int, [P]),
+    "sfem_pattern_build": (C.c_int, [P, P, I64P, I64P]),
+    "sfem_assemble": (C.c_int, [P, P, C.c_int, P, I64, P, I64, C.c_int, PP]),
+    "sfem_assemble_system": (C.c_int, [P, I64, P, I64, P, I64, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       P, P, I64, P, I64, C.c_int, C.c_int, PP, I64P, I64P]),
+    "sfem_matrix_info": (C.c_int, [P, I64P, I64P]),
+    "sfem_matrix_export_csc": (C.c_int, [P, P, P, P, P, C.c_int]),
+    "sfem_matrix_destroy": (C.c_int, [P]),
+    "sfem_solve_opts_default": (None, [C.POINTER(SolveOpts)]),
+    "sfem_solve_dirichlet": (C.c_int, [P, P, P, I64, P, P, P, C.c_int, C.POINTER(SolveOpts),
+                                       C.POINTER(SolveStats)]),
+}
+
+
+def lib():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing; build it with "
+                               "`python smearfem.jl_gb300/build.py` (nvcc, sm_103a)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code, ctx=None):
+    if code != SFEM_OK:
+        msg = lib().sfem_last_error(ctx).decode() if ctx else ""
+        raise SfemError(code, msg)

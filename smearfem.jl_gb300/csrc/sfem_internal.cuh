@@ -1,0 +1,121 @@
+// Internal declarations shared by the CUDA translation units of
+// libsmearfem_gpu.so.  Nothing here is part of the C ABI.
+//
+// Device data layout (all in HBM, one mesh):
+//   X        double [nN][ndim]                node coordinates (Julia's NodeList order)
+//   ien      int32  [nen][nEl]                0-based node ids, element index fastest
+//   id       int32  [b][nN]                   0-based global DOF of (node, component)
+//   n2e      node -> incident elements, CSR (n2e_ptr int64 [nN+1], n2e int32),
+//            each list sorted ascending (the reference's duplicate-sum order)
+//   pattern  node-block rows in sliced-ELL form (SELL-32): 32 consecutive
+//            nodes form a slice; slice s owns slabs sliceptr[s] ..
+//            sliceptr[s+1]-1; slab k of a slice holds the k-th (ascending)
+//            neighbour of each of its 32 rows:
+//              col [slab*32 + lane]                      int32 neighbour node
+//              val [(slab*b*b + i*b + j)*32 + lane]      b x b block, row-major
+//            Rows shorter than their slice are padded with (own node, 0).
+//   rowptr   int64 [nN+1]  CSR offsets of the node-block rows (export order)
+//   g2i      int32 [n]     global DOF (0-based) -> internal index node*b + comp
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "smearfem_gpu.h"
+
+#define SFEM_VERSION "smearfem-gb300 0.1.0 (sm_103a)"
+
+struct DevErr {
+    int code;          // first error wins (atomicCAS from 0)
+    int aux;
+    long long index;   // offending element / node / DOF
+    unsigned long long neg_det;   // Gauss points with det J < 0 (diagnostic)
+};
+
+struct sfem_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevErr *d_err = nullptr;
+    DevErr *h_err = nullptr;    // pinned
+    void *h_small = nullptr;    // pinned scratch for small read-backs (4 KB)
+    std::string last_error;
+    long long launches = 0;     // kernels launched through the library
+};
+
+struct sfem_mesh {
+    sfem_ctx *ctx = nullptr;
+    int refcnt = 1;
+    int ndim = 0, nen = 0, fclass = 0, b = 1;
+    int64_t ne = 0, nEl = 0, nN = 0;
+    double *X = nullptr;
+    int *ien = nullptr;
+    int *id = nullptr;
+    // pattern
+    bool has_pattern = false;
+    int64_t n_global = 0, nnzb = 0, nslices = 0, nslabs = 0;
+    int64_t *n2e_ptr = nullptr;
+    int *n2e = nullptr;
+    int *rowlen = nullptr;
+    int64_t *rowptr = nullptr;
+    int64_t *sliceptr = nullptr;
+    int *col = nullptr;
+    int *g2i = nullptr;
+    unsigned long long neg_det = 0;
+};
+
+struct sfem_matrix {
+    sfem_mesh *mesh = nullptr;
+    int plane = 0;
+    double *val = nullptr;     // FP64 blocks, SELL layout
+    float *val32 = nullptr;    // FP32 copy (mixed precision), built on demand
+    int64_t n = 0, nnz = 0;
+};
+
+// ---- host-side error helpers (sfem_ctx.cu) -------------------------------
+int sfem_set_error(sfem_ctx *ctx, int code, const char *fmt, ...);
+int sfem_cuda_status(sfem_ctx *ctx, cudaError_t e, const char *what);
+// Synchronise the stream, read the device error word, reset it.
+int sfem_check_device(sfem_ctx *ctx, const char *where);
+int sfem_dalloc(sfem_ctx *ctx, void **p, size_t bytes, const char *what);
+void sfem_dfree(sfem_ctx *ctx, void *p);
+// SFEM_BAD_ARG unless p is NULL or lives in the declared memory space.
+int sfem_check_ptr(sfem_ctx *ctx, const void *p, int mem_space);
+int sfem_copy_in(sfem_ctx *ctx, void *dst, const void *src, size_t bytes, int mem_space);
+int sfem_copy_out(sfem_ctx *ctx, void *dst, const void *src, size_t bytes, int mem_space);
+// Exclusive scan of n int32 (or int64) values into out[0..n], out[n] = total.
+int sfem_scan_i32(sfem_ctx *ctx, const int *in, int64_t *out, int64_t n);
+int sfem_scan_i64(sfem_ctx *ctx, const int64_t *in, int64_t *out, int64_t n);
+void sfem_mesh_release(sfem_mesh *m);
+
+#define SFEM_TRY(...)                     \
+    do {                                  \
+        int _st = (__VA_ARGS__);          \
+        if (_st != SFEM_OK) return _st;   \
+    } while (0)
+
+#define SFEM_CUDA(ctx, expr) SFEM_TRY(sfem_cuda_status((ctx), (expr), #expr))
+
+#define SFEM_LAUNCHED(ctx) ((ctx)->launches++)
+
+// ---- device helpers -------------------------------------------------------
+__device__ __forceinline__ void sfem_dev_error(DevErr *e, int code, long long index) {
+    if (atomicCAS(&e->code, 0, code) == 0) e->index = index;
+}
+
+__host__ __device__ __forceinline__ int64_t sfem_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// number of node pairs a <= b in an element with nen nodes, and their index
+__host__ __device__ __forceinline__ int sfem_npairs(int nen) { return nen * (nen + 1) / 2; }
+__host__ __device__ __forceinline__ int sfem_pair(int a, int b, int nen) {
+    return a * nen - a * (a - 1) / 2 + (b - a);
+}
+
+// Element stiffness buffer produced by the element kernel and consumed by the
+// slot gather: for pair p = (a <= b), block entry (i, j) of element e lives at
+//   kbuf[((size_t)p * B * B + i * B + j) * nEl + e]
+int sfem_element_stiffness(sfem_ctx *ctx, const sfem_mesh *m, int plane, const double *dYoung,
+                           int64_t nYoung, const double *dnu, int64_t nNu, double *kbuf);
+int sfem_gather_blocks(sfem_ctx *ctx, const sfem_mesh *m, const double *kbuf, double *val,
+                       float *val32);

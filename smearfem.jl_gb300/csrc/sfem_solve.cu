@@ -1,0 +1,878 @@
+// Dirichlet elimination and preconditioned CG (examples/vector3D.jl:314-322).
+//
+// The reference forms K_free = C'KC and inverts it densely.  Here the
+// elimination is implicit: vectors keep every internal DOF, constrained DOFs
+// are held at zero by a mask applied in the SpMV and the preconditioner, so
+// CG on the full-length vectors performs exactly the arithmetic of CG on
+// K_free.  The right-hand side is the lift C'(f - K q_d) and the result is
+// q_d + C q_f.
+//
+// Kernels (all on the context stream):
+//   k_spmv       y = mask .* (K x), sliced-ELL node-block rows, one lane per
+//                node row, b x b block FMAs, coalesced 32-lane value loads;
+//                optionally fuses the dot product x.y (the CG denominator)
+//   k_update     x += alpha p, r -= alpha q, z = M^-1 r (Jacobi or nodal
+//                block-Jacobi), fused r.z and r.r
+//   k_update_p   p = z + beta p
+// Global reductions are deterministic: each CTA writes a partial, the last
+// CTA to arrive (atomic ticket) sums all partials in a fixed order and
+// updates the CG scalars on the device, so the host only polls a flag once
+// per chunk of iterations.  Nothing in these kernels waits on another CTA.
+//
+// Precision modes: SFEM_FP64 runs everything in FP64.  SFEM_MIXED runs the
+// CG recurrences (matrix values, vectors, preconditioner, SpMV accumulation)
+// in FP32 and keeps FP64 for the accumulated solution, the true residual
+// b - K x (FP64 SpMV) and the Dirichlet lift: whenever the FP32 residual
+// has dropped by `reliable_delta` since the last refresh, the FP32 iterate
+// is folded into the FP64 solution and the residual is recomputed in FP64
+// (iterative refinement that keeps the Krylov direction p).
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <vector>
+
+#include "sfem_internal.cuh"
+
+namespace {
+
+constexpr int SPMV_T = 256;
+constexpr int UPD_T = 256;
+
+struct CgScalars {
+    double rz, rz_prev, pAp, alpha, beta, rr, bb, tol2, rr_ref;
+    int it, done, status, maxit;
+    unsigned int ticket[4];
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-reduce (a, b), publish the block partials, and let the last CTA sum
+// all partials in a fixed order.  Returns true in every thread of the last
+// CTA, with the totals in *ta / *tb (valid in thread 0).
+__device__ bool reduce2_last(double a, double b, double *partial, unsigned int *ticket, double *ta, double *tb) {
+    __shared__ double sa[32], sb[32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (lane == 0) {
+        sa[warp] = a;
+        sb[warp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0, y = 0;
+        for (int w = 0; w < nw; ++w) {
+            x += sa[w];
+            y += sb[w];
+        }
+        partial[2 * blockIdx.x] = x;
+        partial[2 * blockIdx.x + 1] = y;
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double x = 0, y = 0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+        x += __ldcg(&partial[2 * i]);
+        y += __ldcg(&partial[2 * i + 1]);
+    }
+    x = warp_sum(x);
+    y = warp_sum(y);
+    __syncthreads();
+    if (lane == 0) {
+        sa[warp] = x;
+        sb[warp] = y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double X = 0, Y = 0;
+        for (int w = 0; w < nw; ++w) {
+            X += sa[w];
+            Y += sb[w];
+        }
+        *ta = X;
+        *tb = Y;
+        *ticket = 0;
+    }
+    return true;
+}
+
+// y = mask .* (K x); MODE 1 additionally reduces x.y into pAp and sets alpha.
+template <typename T, int B, int MODE>
+__global__ void __launch_bounds__(SPMV_T)
+k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val, int64_t nN,
+       int64_t nslices, const T *__restrict__ x, T *__restrict__ y, const unsigned char *__restrict__ fixed,
+       CgScalars *S, double *partial) {
+    if (MODE == 1 && S->done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double dot = 0.0;
+    if (s < nslices) {
+        const int64_t r = s * 32 + lane;
+        const int64_t slab0 = sliceptr[s], slab1 = sliceptr[s + 1];
+        T acc[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) acc[i] = T(0);
+        const int *cp = col + slab0 * 32 + lane;
+        const T *vp = val + slab0 * (32 * B * B) + lane;
+#pragma unroll 2
+        for (int64_t k = slab0; k < slab1; ++k) {
+            const int c = __ldg(cp);
+            T v[B * B];
+#pragma unroll
+            for (int i = 0; i < B * B; ++i) v[i] = __ldg(vp + i * 32);
+            T xc[B];
+#pragma unroll
+            for (int j = 0; j < B; ++j) xc[j] = __ldg(&x[(int64_t)c * B + j]);
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) acc[i] = fma(v[i * B + j], xc[j], acc[i]);
+            cp += 32;
+            vp += 32 * B * B;
+        }
+        if (r < nN) {
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                const int64_t d = r * B + i;
+                const T out = fixed[d] ? T(0) : acc[i];
+                y[d] = out;
+                if (MODE == 1) dot += (double)(x[d] * out);
+            }
+        }
+    }
+    if (MODE == 1) {
+        double tot, dummy;
+        if (reduce2_last(dot, 0.0, partial, &S->ticket[0], &tot, &dummy) && threadIdx.x == 0) {
+            S->pAp = tot;
+            if (!(tot > 0.0)) {  // K_free not positive definite along p (or NaN)
+                S->status = SFEM_SINGULAR;
+                S->done = 1;
+                S->alpha = 0.0;
+            } else {
+                S->alpha = S->rz / tot;
+            }
+        }
+    }
+}
+
+// x += alpha p; r -= alpha q; z = M^-1 r; reduce r.z and r.r; CG scalar update.
+// PC: 0 Jacobi (minv per DOF), 1 block-Jacobi (minv: B x B per node).
+template <typename T, int B, int PC>
+__global__ void __launch_bounds__(UPD_T)
+k_update(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
+         const T *__restrict__ q, const T *__restrict__ minv, CgScalars *S, double *partial) {
+    if (S->done) return;
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double rz = 0.0, rr = 0.0;
+    if (node < nN) {
+        const T alpha = (T)S->alpha;
+        T rv[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const int64_t d = node * B + i;
+            x[d] = fma(alpha, p[d], x[d]);
+            rv[i] = fma(-alpha, q[d], r[d]);
+            r[d] = rv[i];
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            T zi;
+            if (PC == 0) {
+                zi = minv[node * B + i] * rv[i];
+            } else {
+                zi = T(0);
+#pragma unroll
+                for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], rv[j], zi);
+            }
+            z[node * B + i] = zi;
+            rz += (double)(rv[i] * zi);
+            rr += (double)(rv[i] * rv[i]);
+        }
+    }
+    double trz, trr;
+    if (reduce2_last(rz, rr, partial, &S->ticket[1], &trz, &trr) && threadIdx.x == 0) {
+        S->rr = trr;
+        S->it += 1;
+        S->rz_prev = S->rz;
+        S->rz = trz;
+        S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        if (trr <= S->tol2) {
+            S->done = 1;
+            S->status = SFEM_OK;
+        } else if (S->it >= S->maxit) {
+            S->done = 1;
+            S->status = SFEM_NOT_CONVERGED;
+        } else if (!(trr == trr)) {
+            S->done = 1;
+            S->status = SFEM_SINGULAR;
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_update_p(int64_t n, T *__restrict__ p, const T *__restrict__ z, const CgScalars *S) {
+    if (S->done) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = fma((T)S->beta, p[i], z[i]);
+}
+
+// ---- set-up kernels --------------------------------------------------------
+
+// Mark every internal DOF of a node no element uses as fixed (it is not in K).
+__global__ void k_mask_inactive(const int *__restrict__ rowlen, int64_t nN, int b, unsigned char *__restrict__ fixed) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nN * b) return;
+    fixed[t] = rowlen[t / b] == 0 ? 1 : 0;
+}
+
+__global__ void k_fix(const int64_t *__restrict__ dofs, const double *__restrict__ vals, int64_t nfix, int64_t n,
+                      const int *__restrict__ g2i, unsigned char *__restrict__ fixed, double *__restrict__ ud,
+                      unsigned char *__restrict__ gfixed, DevErr *err) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nfix) return;
+    const int64_t g = dofs[t] - 1;
+    if (g < 0 || g >= n) {
+        sfem_dev_error(err, SFEM_BAD_INDEX, t);
+        return;
+    }
+    gfixed[g] = 1;
+    const int i = g2i[g];
+    if (i < 0) return;  // empty row/column of K
+    fixed[i] = 1;
+    ud[i] = vals[t];
+}
+
+// Internal vector from a global one (f), zero where no global DOF maps.
+__global__ void k_gather_global(const double *__restrict__ fg, int64_t n, const int *__restrict__ g2i,
+                                double *__restrict__ fi) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int i = g2i[g];
+    if (i >= 0) fi[i] = fg[g];
+}
+
+// b = f - K ud on free DOFs (0 on fixed).
+__global__ void k_rhs(int64_t nd, const double *__restrict__ f, const double *__restrict__ Kud,
+                      const unsigned char *__restrict__ fixed, double *__restrict__ bvec) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nd) return;
+    bvec[i] = fixed[i] ? 0.0 : (f ? f[i] : 0.0) - Kud[i];
+}
+
+// Global DOFs that are free but have no row in K make K_free singular.
+__global__ void k_check_empty(int64_t n, const int *__restrict__ g2i, const unsigned char *__restrict__ gfixed,
+                              DevErr *err) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    if (g2i[g] < 0 && !gfixed[g]) sfem_dev_error(err, SFEM_SINGULAR, g);
+}
+
+// Preconditioner from the diagonal blocks.  PC 0: 1/K_ii; PC 1: inverse of the
+// node's b x b block restricted to its free components.
+template <typename T, int B, int PC>
+__global__ void k_precond(const int64_t *__restrict__ sliceptr, const int *__restrict__ col,
+                          const double *__restrict__ val, const int *__restrict__ rowlen, int64_t nN,
+                          const unsigned char *__restrict__ fixed, T *__restrict__ minv, DevErr *err) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nN) return;
+    double D[B][B];
+    for (int i = 0; i < B; ++i)
+        for (int j = 0; j < B; ++j) D[i][j] = 0.0;
+    const int len = rowlen[node];
+    const int64_t s = node >> 5;
+    const int lane = (int)(node & 31);
+    const int64_t slab0 = sliceptr[s];
+    for (int k = 0; k < len; ++k) {
+        const int64_t slab = slab0 + k;
+        if (col[slab * 32 + lane] == (int)node) {
+            for (int i = 0; i < B; ++i)
+                for (int j = 0; j < B; ++j) D[i][j] = val[(slab * B * B + i * B + j) * 32 + lane];
+            break;
+        }
+    }
+    bool fx[B];
+    bool any_free = false;
+    for (int i = 0; i < B; ++i) {
+        fx[i] = fixed[node * B + i] != 0;
+        any_free |= !fx[i];
+    }
+    if (PC == 0 || B == 1) {
+        for (int i = 0; i < B; ++i) {
+            T v = T(0);
+            if (!fx[i]) {
+                if (!(D[i][i] != 0.0) || !isfinite(D[i][i])) sfem_dev_error(err, SFEM_SINGULAR, node * B + i);
+                else v = (T)(1.0 / D[i][i]);
+            }
+            if (PC == 0) minv[node * B + i] = v;
+            else minv[(node * B + i) * B + i] = v;
+        }
+        return;
+    }
+    // free-restricted block: fixed rows/cols -> identity, invert, zero them again
+    for (int i = 0; i < B; ++i)
+        for (int j = 0; j < B; ++j)
+            if (fx[i] || fx[j]) D[i][j] = (i == j) ? 1.0 : 0.0;
+    double I[B][B];
+    double det;
+    if (B == 2) {
+        det = D[0][0] * D[1][1] - D[0][1] * D[1][0];
+        I[0][0] = D[1][1];
+        I[0][1] = -D[0][1];
+        I[1][0] = -D[1][0];
+        I[1][1] = D[0][0];
+    } else {
+        I[0][0] = D[1][1] * D[2][2] - D[1][2] * D[2][1];
+        I[0][1] = D[0][2] * D[2][1] - D[0][1] * D[2][2];
+        I[0][2] = D[0][1] * D[1][2] - D[0][2] * D[1][1];
+        I[1][0] = D[1][2] * D[2][0] - D[1][0] * D[2][2];
+        I[1][1] = D[0][0] * D[2][2] - D[0][2] * D[2][0];
+        I[1][2] = D[0][2] * D[1][0] - D[0][0] * D[1][2];
+        I[2][0] = D[1][0] * D[2][1] - D[1][1] * D[2][0];
+        I[2][1] = D[0][1] * D[2][0] - D[0][0] * D[2][1];
+        I[2][2] = D[0][0] * D[1][1] - D[0][1] * D[1][0];
+        det = D[0][0] * I[0][0] + D[0][1] * I[1][0] + D[0][2] * I[2][0];
+    }
+    if (any_free && (!(det != 0.0) || !isfinite(det))) sfem_dev_error(err, SFEM_SINGULAR, node * B);
+    const double rdet = det != 0.0 ? 1.0 / det : 0.0;
+    for (int i = 0; i < B; ++i)
+        for (int j = 0; j < B; ++j)
+            minv[(node * B + i) * B + j] = (fx[i] || fx[j]) ? T(0) : (T)(I[i][j] * rdet);
+}
+
+// u_global[g] = ud[i] + x[i]  (or the prescribed value for DOFs outside K)
+__global__ void k_scatter_out(int64_t n, const int *__restrict__ g2i, const double *__restrict__ ud,
+                              const double *__restrict__ x, double *__restrict__ ug) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int i = g2i[g];
+    ug[g] = i >= 0 ? ud[i] + x[i] : 0.0;
+}
+
+__global__ void k_fixed_out(const int64_t *__restrict__ dofs, const double *__restrict__ vals, int64_t nfix,
+                            const int *__restrict__ g2i, double *__restrict__ ug) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nfix) return;
+    const int64_t g = dofs[t] - 1;
+    if (g2i[g] < 0) ug[g] = vals[t];
+}
+
+// ---- mixed-precision glue ---------------------------------------------------
+
+template <typename T>
+__global__ void k_cast(int64_t n, const double *__restrict__ a, T *__restrict__ b) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (T)a[i];
+}
+
+__global__ void k_fold(int64_t n, double *__restrict__ x64, float *__restrict__ x32) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x64[i] += (double)x32[i];
+    x32[i] = 0.0f;
+}
+
+// r64 = b - Kx64 (masked), r32 = (float) r64, z32 = M^-1 r32; reduce r.z, r.r.
+template <int B, int PC>
+__global__ void __launch_bounds__(UPD_T)
+k_refresh(int64_t nN, const double *__restrict__ bvec, const double *__restrict__ Kx, const unsigned char *__restrict__ fixed,
+          double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ z32, const float *__restrict__ minv,
+          CgScalars *S, double *partial) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double rz = 0.0, rr = 0.0;
+    if (node < nN) {
+        float rv[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const int64_t d = node * B + i;
+            const double v = fixed[d] ? 0.0 : bvec[d] - Kx[d];
+            r64[d] = v;
+            rv[i] = (float)v;
+            r32[d] = rv[i];
+            rr += v * v;
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            float zi;
+            if (PC == 0) {
+                zi = minv[node * B + i] * rv[i];
+            } else {
+                zi = 0.0f;
+#pragma unroll
+                for (int j = 0; j < B; ++j) zi = fmaf(minv[(node * B + i) * B + j], rv[j], zi);
+            }
+            z32[node * B + i] = zi;
+            rz += (double)(rv[i] * zi);
+        }
+    }
+    double trz, trr;
+    if (reduce2_last(rz, rr, partial, &S->ticket[2], &trz, &trr) && threadIdx.x == 0) {
+        S->rr = trr;
+        S->rr_ref = trr;
+        S->rz = trz;
+        S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        if (trr <= S->tol2) {
+            S->done = 1;
+            S->status = SFEM_OK;
+        } else {
+            S->done = 0;
+            S->status = SFEM_NOT_CONVERGED;
+        }
+    }
+}
+
+// ||mask .* (b - K x)||^2 into S->rr (final true residual of the FP64 path)
+__global__ void __launch_bounds__(UPD_T)
+k_true_residual(int64_t nd, const double *__restrict__ bvec, const double *__restrict__ Kx,
+                const unsigned char *__restrict__ fixed, CgScalars *S, double *partial) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0;
+    if (i < nd && !fixed[i]) {
+        const double v = bvec[i] - Kx[i];
+        rr = v * v;
+    }
+    double t, dummy;
+    if (reduce2_last(rr, 0.0, partial, &S->ticket[2], &t, &dummy) && threadIdx.x == 0) S->rr = t;
+}
+
+// initial z = M^-1 r and rz, rr (FP64 or FP32 vectors)
+template <typename T, int B, int PC>
+__global__ void __launch_bounds__(UPD_T)
+k_init(int64_t nN, const T *__restrict__ r, T *__restrict__ z, T *__restrict__ p, const T *__restrict__ minv,
+       CgScalars *S, double *partial) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double rz = 0.0, rr = 0.0;
+    if (node < nN) {
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const int64_t d = node * B + i;
+            T zi;
+            if (PC == 0) {
+                zi = minv[d] * r[d];
+            } else {
+                zi = T(0);
+#pragma unroll
+                for (int j = 0; j < B; ++j) zi = fma(minv[d * B + j], r[node * B + j], zi);
+            }
+            z[d] = zi;
+            p[d] = T(0);
+            rz += (double)(r[d] * zi);
+            rr += (double)r[d] * (double)r[d];
+        }
+    }
+    double trz, trr;
+    if (reduce2_last(rz, rr, partial, &S->ticket[3], &trz, &trr) && threadIdx.x == 0) {
+        S->rz = trz;
+        S->rz_prev = trz;
+        S->rr = trr;
+        S->rr_ref = trr;
+        S->beta = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct Vecs {
+    T *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *minv = nullptr;
+};
+
+class Solver {
+   public:
+    Solver(sfem_ctx *c, sfem_matrix *K, const sfem_solve_opts &o) : ctx(c), K(K), m(K->mesh), opts(o) {}
+    ~Solver() {
+        for (void *p : owned) sfem_dfree(ctx, p);
+        if (gexec) cudaGraphExecDestroy(gexec);
+        for (auto &e : events) cudaEventDestroy(e);
+        cudaStreamSynchronize(ctx->stream);
+    }
+
+    int run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_vals, const double *f, double *u_out,
+            int mem_space, sfem_solve_stats *stats);
+
+   private:
+    template <typename T>
+    int alloc(T **p, int64_t n, const char *what) {
+        SFEM_TRY(sfem_dalloc(ctx, (void **)p, sizeof(T) * (n > 0 ? n : 1), what));
+        owned.push_back(*p);
+        return SFEM_OK;
+    }
+    template <int B>
+    int solve_b(double *x64_out);
+    template <typename T, int B, int PC>
+    int cg_loop(Vecs<T> &v, bool mixed, double *x64, double *r64, double *q64);
+    template <typename T, int B>
+    void launch_spmv(const T *val, const T *x, T *y, bool fused);
+    int read_scalars(CgScalars *h);
+
+    sfem_ctx *ctx;
+    sfem_matrix *K;
+    sfem_mesh *m;
+    sfem_solve_opts opts;
+    std::vector<void *> owned;
+    unsigned char *fixed = nullptr, *gfixed = nullptr;
+    double *ud = nullptr, *bvec = nullptr, *partial = nullptr;
+    CgScalars *S = nullptr;
+    int64_t nd = 0;  // internal DOFs = nN * b
+    unsigned spmv_grid = 1, upd_grid = 1, vec_grid = 1;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<cudaEvent_t> events;
+    double ms_spmv = 0.0;
+    int spmv_timed = 0;
+    int reliable = 0;
+    int iterations = 0;
+    int status = SFEM_OK;
+    double relres = 0.0;
+};
+
+template <typename T, int B>
+void Solver::launch_spmv(const T *val, const T *x, T *y, bool fused) {
+    if (fused)
+        k_spmv<T, B, 1><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(m->sliceptr, m->col, val, m->nN, m->nslices, x, y,
+                                                               fixed, S, partial);
+    else
+        k_spmv<T, B, 0><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(m->sliceptr, m->col, val, m->nN, m->nslices, x, y,
+                                                               fixed, S, partial);
+    SFEM_LAUNCHED(ctx);
+}
+
+int Solver::read_scalars(CgScalars *h) {
+    SFEM_CUDA(ctx, cudaMemcpyAsync(h, S, sizeof(CgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+    SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SFEM_OK;
+}
+
+template <typename T, int B, int PC>
+int Solver::cg_loop(Vecs<T> &v, bool mixed, double *x64, double *r64, double *q64) {
+    const T *val = nullptr;
+    if constexpr (sizeof(T) == 8) val = (const T *)K->val;
+    else val = (const T *)K->val32;
+    CgScalars *h = (CgScalars *)ctx->h_small;
+    const int chunk = opts.check_every > 0 ? opts.check_every : 32;
+    const bool profile = opts.profile != 0;
+    auto enqueue_iter = [&](int slot) {
+        k_update_p<T><<<vec_grid, 256, 0, ctx->stream>>>(nd, v.p, v.z, S);
+        SFEM_LAUNCHED(ctx);
+        if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
+        launch_spmv<T, B>(val, v.p, v.q, true);
+        if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
+        k_update<T, B, PC><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.x, v.r, v.z, v.p, v.q, v.minv, S, partial);
+        SFEM_LAUNCHED(ctx);
+    };
+    if (profile) {
+        events.resize(2 * chunk);
+        for (auto &e : events) SFEM_CUDA(ctx, cudaEventCreate(&e));
+    } else {
+        cudaGraph_t g;
+        const long long before = ctx->launches;
+        SFEM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < chunk; ++i) enqueue_iter(i);
+        SFEM_CUDA(ctx, cudaStreamEndCapture(ctx->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+        cudaGraphDestroy(g);
+        SFEM_CUDA(ctx, e);
+        ctx->launches = before;  // counted per graph launch below
+    }
+    int it_prev = 0;
+    const double delta2 = opts.reliable_delta * opts.reliable_delta;
+    int guard = 0;
+    while (true) {
+        if (profile) {
+            for (int i = 0; i < chunk; ++i) enqueue_iter(i);
+        } else {
+            SFEM_CUDA(ctx, cudaGraphLaunch(gexec, ctx->stream));
+            ctx->launches += 3 * chunk;
+        }
+        SFEM_TRY(read_scalars(h));
+        if (profile) {
+            // only the iterations that ran (kernels after convergence exit at once)
+            const int ran = std::min(chunk, std::max(0, h->it - it_prev));
+            for (int i = 0; i < ran; ++i) {
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, events[2 * i], events[2 * i + 1]) == cudaSuccess) {
+                    ms_spmv += ms;
+                    spmv_timed++;
+                }
+            }
+        }
+        if (mixed) {
+            const bool conv = h->done && h->status == SFEM_OK;
+            const bool drop = h->rr <= delta2 * h->rr_ref;
+            if ((conv || drop || (h->done && h->status == SFEM_NOT_CONVERGED && h->it >= h->maxit)) &&
+                h->status != SFEM_SINGULAR) {
+                // FP64 refresh: x64 += x32, r = b - K x64, restart the recurrences from it
+                k_fold<<<vec_grid, 256, 0, ctx->stream>>>(nd, x64, (float *)v.x);
+                SFEM_LAUNCHED(ctx);
+                launch_spmv<double, B>(K->val, x64, q64, false);
+                k_refresh<B, PC><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, bvec, q64, fixed, r64, (float *)v.r,
+                                                                      (float *)v.z, (const float *)v.minv, S, partial);
+                SFEM_LAUNCHED(ctx);
+                reliable++;
+                SFEM_TRY(read_scalars(h));
+                it_prev = h->it;
+                if (h->done && h->status == SFEM_OK) break;
+                if (h->it >= h->maxit) {
+                    h->status = SFEM_NOT_CONVERGED;
+                    break;
+                }
+                continue;
+            }
+        }
+        if (h->done) break;
+        it_prev = h->it;
+        if (++guard > (1 << 30)) break;
+    }
+    iterations = h->it;
+    status = h->status;
+    if constexpr (sizeof(T) == 8) {
+        if (status != SFEM_SINGULAR) {
+            // report the true FP64 residual of the returned iterate
+            launch_spmv<double, B>(K->val, v.x, v.q, false);
+            k_true_residual<<<vec_grid, UPD_T, 0, ctx->stream>>>(nd, bvec, v.q, fixed, S, partial);
+            SFEM_LAUNCHED(ctx);
+            SFEM_TRY(read_scalars(h));
+        }
+    }
+    relres = h->bb > 0 ? sqrt(h->rr / h->bb) : 0.0;
+    return SFEM_OK;
+}
+
+template <int B>
+int Solver::solve_b(double *x64) {
+    const bool mixed = opts.precision == SFEM_MIXED;
+    const bool block = opts.precond == SFEM_PC_BLOCK_JACOBI && B > 1;
+    const int mwidth = block ? B * B : B;
+    // FP64 preconditioner inverse is built first, then cast for the FP32 path
+    double *minv64 = nullptr;
+    SFEM_TRY(alloc(&minv64, m->nN * mwidth, "preconditioner"));
+    if (block)
+        k_precond<double, B, 1><<<(unsigned)sfem_cdiv(m->nN, 256), 256, 0, ctx->stream>>>(
+            m->sliceptr, m->col, K->val, m->rowlen, m->nN, fixed, minv64, ctx->d_err);
+    else
+        k_precond<double, B, 0><<<(unsigned)sfem_cdiv(m->nN, 256), 256, 0, ctx->stream>>>(
+            m->sliceptr, m->col, K->val, m->rowlen, m->nN, fixed, minv64, ctx->d_err);
+    SFEM_LAUNCHED(ctx);
+    SFEM_TRY(sfem_check_device(ctx, "preconditioner"));
+
+    if (!mixed) {
+        Vecs<double> v;
+        v.x = x64;
+        SFEM_TRY(alloc(&v.r, nd, "r"));
+        SFEM_TRY(alloc(&v.z, nd, "z"));
+        SFEM_TRY(alloc(&v.p, nd, "p"));
+        SFEM_TRY(alloc(&v.q, nd, "q"));
+        v.minv = minv64;
+        SFEM_CUDA(ctx, cudaMemcpyAsync(v.r, bvec, sizeof(double) * nd, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (block)
+            k_init<double, B, 1><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
+        else
+            k_init<double, B, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
+        SFEM_LAUNCHED(ctx);
+        SFEM_TRY(block ? cg_loop<double, B, 1>(v, false, nullptr, nullptr, nullptr)
+                       : cg_loop<double, B, 0>(v, false, nullptr, nullptr, nullptr));
+    } else {
+        if (!K->val32) {
+            const int64_t nv = m->nslabs * 32 * B * B;
+            SFEM_TRY(sfem_dalloc(ctx, (void **)&K->val32, sizeof(float) * (nv ? nv : 1), "FP32 K values"));
+            k_cast<float><<<(unsigned)sfem_cdiv(nv > 0 ? nv : 1, 256), 256, 0, ctx->stream>>>(nv, K->val, K->val32);
+            SFEM_LAUNCHED(ctx);
+        }
+        Vecs<float> v;
+        SFEM_TRY(alloc(&v.x, nd, "x32"));
+        SFEM_TRY(alloc(&v.r, nd, "r32"));
+        SFEM_TRY(alloc(&v.z, nd, "z32"));
+        SFEM_TRY(alloc(&v.p, nd, "p32"));
+        SFEM_TRY(alloc(&v.q, nd, "q32"));
+        SFEM_TRY(alloc(&v.minv, m->nN * mwidth, "minv32"));
+        double *r64 = nullptr, *q64 = nullptr;
+        SFEM_TRY(alloc(&r64, nd, "r64"));
+        SFEM_TRY(alloc(&q64, nd, "q64"));
+        SFEM_CUDA(ctx, cudaMemsetAsync(v.x, 0, sizeof(float) * nd, ctx->stream));
+        k_cast<float><<<(unsigned)sfem_cdiv(m->nN * mwidth, 256), 256, 0, ctx->stream>>>(m->nN * mwidth, minv64,
+                                                                                           v.minv);
+        k_cast<float><<<vec_grid, 256, 0, ctx->stream>>>(nd, bvec, v.r);
+        SFEM_LAUNCHED(ctx);
+        SFEM_LAUNCHED(ctx);
+        if (block)
+            k_init<float, B, 1><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
+        else
+            k_init<float, B, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
+        SFEM_LAUNCHED(ctx);
+        SFEM_TRY(block ? cg_loop<float, B, 1>(v, true, x64, r64, q64) : cg_loop<float, B, 0>(v, true, x64, r64, q64));
+    }
+    return SFEM_OK;
+}
+
+int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_vals, const double *f, double *u_out,
+                int mem_space, sfem_solve_stats *stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    const int b = m->b;
+    const int64_t n = K->n;
+    nd = m->nN * b;
+    spmv_grid = (unsigned)sfem_cdiv(m->nslices * 32 > 0 ? m->nslices * 32 : 1, SPMV_T);
+    upd_grid = (unsigned)sfem_cdiv(m->nN, UPD_T);
+    vec_grid = (unsigned)sfem_cdiv(nd, 256);
+    const long long launches0 = ctx->launches;
+
+    int64_t *dfix = nullptr;
+    double *dvals = nullptr, *fg = nullptr, *fi = nullptr, *x64 = nullptr, *ug = nullptr;
+    SFEM_TRY(alloc(&fixed, nd, "fixed mask"));
+    SFEM_TRY(alloc(&gfixed, n, "global fixed mask"));
+    SFEM_TRY(alloc(&ud, nd, "q_d"));
+    SFEM_TRY(alloc(&bvec, nd, "rhs"));
+    SFEM_TRY(alloc(&x64, nd, "x"));
+    SFEM_TRY(alloc(&ug, n, "u"));
+    SFEM_TRY(alloc(&S, 1, "CG scalars"));
+    SFEM_TRY(alloc(&partial, 2 * (int64_t)std::max(spmv_grid, std::max(upd_grid, vec_grid)), "partials"));
+    SFEM_TRY(alloc(&dfix, nfix, "fixed dofs"));
+    SFEM_TRY(alloc(&dvals, nfix, "fixed values"));
+    SFEM_TRY(sfem_copy_in(ctx, dfix, fixed_dofs, sizeof(int64_t) * nfix, mem_space));
+    SFEM_TRY(sfem_copy_in(ctx, dvals, fixed_vals, sizeof(double) * nfix, mem_space));
+    SFEM_CUDA(ctx, cudaMemsetAsync(ud, 0, sizeof(double) * nd, ctx->stream));
+    SFEM_CUDA(ctx, cudaMemsetAsync(x64, 0, sizeof(double) * nd, ctx->stream));
+    SFEM_CUDA(ctx, cudaMemsetAsync(gfixed, 0, n > 0 ? n : 1, ctx->stream));
+    k_mask_inactive<<<vec_grid, 256, 0, ctx->stream>>>(m->rowlen, m->nN, b, fixed);
+    SFEM_LAUNCHED(ctx);
+    if (nfix > 0) {
+        k_fix<<<(unsigned)sfem_cdiv(nfix, 256), 256, 0, ctx->stream>>>(dfix, dvals, nfix, n, m->g2i, fixed, ud, gfixed,
+                                                                       ctx->d_err);
+        SFEM_LAUNCHED(ctx);
+    }
+    if (n > 0) {
+        k_check_empty<<<(unsigned)sfem_cdiv(n, 256), 256, 0, ctx->stream>>>(n, m->g2i, gfixed, ctx->d_err);
+        SFEM_LAUNCHED(ctx);
+    }
+    if (f) {
+        SFEM_TRY(alloc(&fg, n, "f"));
+        SFEM_TRY(alloc(&fi, nd, "f internal"));
+        SFEM_TRY(sfem_copy_in(ctx, fg, f, sizeof(double) * n, mem_space));
+        SFEM_CUDA(ctx, cudaMemsetAsync(fi, 0, sizeof(double) * nd, ctx->stream));
+        k_gather_global<<<(unsigned)sfem_cdiv(n, 256), 256, 0, ctx->stream>>>(fg, n, m->g2i, fi);
+        SFEM_LAUNCHED(ctx);
+    }
+    SFEM_TRY(sfem_check_device(ctx, "Dirichlet set-up"));
+    // lift: b = f - K q_d on the free DOFs (q64 of the mixed path reuses x64 as scratch here)
+    {
+        unsigned char *nofix = nullptr;
+        SFEM_TRY(alloc(&nofix, nd, "no mask"));
+        SFEM_CUDA(ctx, cudaMemsetAsync(nofix, 0, nd, ctx->stream));
+        unsigned char *keep = fixed;
+        fixed = nofix;
+        if (b == 1) launch_spmv<double, 1>(K->val, ud, x64, false);
+        else if (b == 2) launch_spmv<double, 2>(K->val, ud, x64, false);
+        else launch_spmv<double, 3>(K->val, ud, x64, false);
+        fixed = keep;
+        k_rhs<<<vec_grid, 256, 0, ctx->stream>>>(nd, fi, x64, fixed, bvec);
+        SFEM_LAUNCHED(ctx);
+        SFEM_CUDA(ctx, cudaMemsetAsync(x64, 0, sizeof(double) * nd, ctx->stream));
+    }
+    // ||b||^2 and the stopping threshold
+    CgScalars hs;
+    memset(&hs, 0, sizeof(hs));
+    hs.maxit = opts.maxit > 0 ? opts.maxit : 1000000;
+    SFEM_CUDA(ctx, cudaMemcpyAsync(S, &hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
+    {
+        // rr of b via k_init on a throwaway z/p: reuse the generic reduction
+        double *tz = nullptr, *tp = nullptr, *ones = nullptr;
+        SFEM_TRY(alloc(&tz, nd, "tmp"));
+        SFEM_TRY(alloc(&tp, nd, "tmp"));
+        SFEM_TRY(alloc(&ones, nd, "tmp"));
+        SFEM_CUDA(ctx, cudaMemsetAsync(ones, 0, sizeof(double) * nd, ctx->stream));
+        if (b == 1) k_init<double, 1, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, bvec, tz, tp, ones, S, partial);
+        else if (b == 2) k_init<double, 2, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, bvec, tz, tp, ones, S, partial);
+        else k_init<double, 3, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, bvec, tz, tp, ones, S, partial);
+        SFEM_LAUNCHED(ctx);
+        SFEM_TRY(read_scalars(&hs));
+    }
+    const double bb = hs.rr;
+    int64_t n_free = 0;
+    {
+        std::vector<unsigned char> hf(nd);
+        SFEM_CUDA(ctx, cudaMemcpyAsync(hf.data(), fixed, nd, cudaMemcpyDeviceToHost, ctx->stream));
+        SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (unsigned char c : hf) n_free += c ? 0 : 1;
+    }
+    hs.bb = bb;
+    hs.tol2 = opts.rtol * opts.rtol * bb;
+    hs.rr = bb;
+    hs.rr_ref = bb;
+    hs.it = 0;
+    hs.done = bb > 0.0 && n_free > 0 ? 0 : 1;
+    hs.status = SFEM_OK;
+    SFEM_CUDA(ctx, cudaMemcpyAsync(S, &hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
+    if (!hs.done) {
+        if (b == 1) SFEM_TRY(solve_b<1>(x64));
+        else if (b == 2) SFEM_TRY(solve_b<2>(x64));
+        else SFEM_TRY(solve_b<3>(x64));
+    }
+    // output: u = q_d + C q_f in global numbering
+    k_scatter_out<<<(unsigned)sfem_cdiv(n > 0 ? n : 1, 256), 256, 0, ctx->stream>>>(n, m->g2i, ud, x64, ug);
+    SFEM_LAUNCHED(ctx);
+    if (nfix > 0) {
+        k_fixed_out<<<(unsigned)sfem_cdiv(nfix, 256), 256, 0, ctx->stream>>>(dfix, dvals, nfix, m->g2i, ug);
+        SFEM_LAUNCHED(ctx);
+    }
+    SFEM_TRY(sfem_copy_out(ctx, u_out, ug, sizeof(double) * n, mem_space));
+    SFEM_TRY(sfem_check_device(ctx, "solve"));
+    auto t1 = std::chrono::steady_clock::now();
+    if (stats) {
+        stats->status = hs.done && iterations == 0 ? SFEM_OK : status;
+        stats->iterations = iterations;
+        stats->reliable_updates = reliable;
+        stats->relres = relres;
+        stats->ms_total = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        stats->ms_spmv = ms_spmv;
+        stats->spmv_launches = spmv_timed;
+        stats->kernel_launches = (int)(ctx->launches - launches0);
+        stats->n_free = n_free;
+    }
+    const int st = hs.done && iterations == 0 ? SFEM_OK : status;
+    if (st == SFEM_NOT_CONVERGED)
+        return sfem_set_error(ctx, st, "CG reached maxit=%d at relative residual %.3e", opts.maxit, relres);
+    if (st == SFEM_SINGULAR) return sfem_set_error(ctx, st, "CG breakdown: K_free is singular or indefinite");
+    return st;
+}
+
+}  // namespace
+
+extern "C" void sfem_solve_opts_default(sfem_solve_opts *o) {
+    if (!o) return;
+    o->precision = SFEM_FP64;
+    o->precond = SFEM_PC_JACOBI;
+    o->rtol = 1e-10;
+    o->maxit = 100000;
+    o->check_every = 32;
+    o->reliable_delta = 0.1;
+    o->profile = 0;
+}
+
+extern "C" int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t *fixed_dofs, int64_t nfix,
+                                    const double *fixed_vals, const double *f, double *u_out, int mem_space,
+                                    const sfem_solve_opts *opts, sfem_solve_stats *stats) {
+    if (!ctx || !K || !u_out) return SFEM_BAD_ARG;
+    if (nfix < 0 || (nfix > 0 && (!fixed_dofs || !fixed_vals))) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad fixed DOF list");
+    cudaSetDevice(ctx->device);
+    sfem_solve_opts o;
+    sfem_solve_opts_default(&o);
+    if (opts) o = *opts;
+    if (!(o.rtol >= 0.0) || o.maxit < 0 || (o.precision != SFEM_FP64 && o.precision != SFEM_MIXED) ||
+        (o.precond != SFEM_PC_JACOBI && o.precond != SFEM_PC_BLOCK_JACOBI) || !(o.reliable_delta > 0.0) ||
+        !(o.reliable_delta < 1.0))
+        return sfem_set_error(ctx, SFEM_BAD_ARG, "bad solve options");
+    if (stats) memset(stats, 0, sizeof(*stats));
+    Solver s(ctx, K, o);
+    return s.run(fixed_dofs, nfix, fixed_vals, f, u_out, mem_space, stats);
+}

@@ -1,0 +1,359 @@
+"""Host-side mirror of smearFEM.jl's FE API over the GB300 C ABI.
+
+Same names, argument meaning and array shapes as the reference
+(src/smearFEM.jl:3 exports ``assemble_system, gaussian_quadrature,
+basis_function``), so code written against the reference reads the same:
+
+  gaussian_quadrature(a, b, nGaussPoints=2)                  src/fem.jl:21-31
+  basis_function(xi, eta=None, zeta=None, FunctionClass="Q1") src/fem.jl:48-114
+  assemble_system(ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1,
+                  ID=None, Young=1, nu=0.3)                   src/fem.jl:135-256
+
+Arrays use the reference's shapes and 1-based indices: ``NodeList`` (ndim,
+nN), ``IEN`` (nEl, nen), ``ID`` (nN, nDof).  ``assemble_system`` returns the
+matrix as ``scipy.sparse.csc_matrix`` (the SparseMatrixCSC of the reference)
+or, with ``as_handle=True``, a :class:`Matrix` that stays on the GPU.  The
+Dirichlet solve of examples/vector3D.jl:314-322 is :func:`solve_dirichlet`.
+
+Errors raise :class:`SfemError` (the reference raises Julia exceptions:
+``BoundsError`` for bad indices, ``SingularException`` from ``inv``).
+Every numeric step runs in libsmearfem_gpu.so on the GPU; nothing here
+computes FE results on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import SfemError, check, lib
+
+try:  # device-resident inputs are optional; torch is only plumbing here
+    import torch as _torch
+except Exception:  # pragma: no cover
+    _torch = None
+
+
+def _is_dev(x):
+    return _torch is not None and isinstance(x, _torch.Tensor) and x.is_cuda
+
+
+class _Buf:
+    """Pointer to an argument in Julia (column-major) memory order."""
+
+    def __init__(self, x, dtype, order="F"):
+        self.keep = None
+        self.space = L.MEM_HOST
+        if x is None:
+            self.ptr = None
+            return
+        if _is_dev(x):
+            tdt = {np.float64: _torch.float64, np.int64: _torch.int64}[dtype]
+            t = x.to(tdt)
+            if t.dim() == 2 and order == "F":
+                t = t.t()
+            t = t.contiguous()
+            self.keep = t
+            self.ptr = C.c_void_p(t.data_ptr())
+            self.space = L.MEM_DEVICE
+            self.size = t.numel()
+            return
+        a = np.asarray(x, dtype=dtype)
+        a = np.ascontiguousarray(a.ravel(order=order))
+        self.keep = a
+        self.size = a.size
+        self.ptr = C.c_void_p(a.ctypes.data) if a.size else None
+
+
+def _space(*bufs):
+    spaces = {b.space for b in bufs if b.ptr is not None}
+    if len(spaces) > 1:
+        raise SfemError(L.SFEM_BAD_ARG, "mix of host and device arrays in one call")
+    return spaces.pop() if spaces else L.MEM_HOST
+
+
+# ---------------------------------------------------------------------------
+# context
+# ---------------------------------------------------------------------------
+
+class Context:
+    """One GPU, one CUDA stream (sfem_ctx_create)."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        code = lib().sfem_ctx_create(int(device), C.byref(h))
+        if code != L.SFEM_OK:
+            raise SfemError(code, f"cannot create a context on CUDA device {device}")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sfem_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        check(lib().sfem_ctx_synchronize(self.h), self.h)
+
+    def error(self):
+        return lib().sfem_last_error(self.h).decode()
+
+
+_contexts = {}
+
+
+def get_context(device=0):
+    ctx = _contexts.get(device)
+    if ctx is None or ctx.h is None:
+        ctx = _contexts[device] = Context(device)
+    return ctx
+
+
+def version():
+    return lib().sfem_version().decode()
+
+
+# ---------------------------------------------------------------------------
+# host helpers (src/fem.jl:21-31, :48-114) -- computed by the library's host code
+# ---------------------------------------------------------------------------
+
+def gaussian_quadrature(a, b, nGaussPoints=2):
+    """Gauss-Legendre nodes and weights on [a, b] (src/fem.jl:21-31)."""
+    xi = np.zeros(max(nGaussPoints, 1))
+    w = np.zeros(max(nGaussPoints, 1))
+    code = lib().sfem_gaussian_quadrature(float(a), float(b), int(nGaussPoints),
+                                          xi.ctypes.data, w.ctypes.data)
+    if code != L.SFEM_OK:
+        raise SfemError(code, "nGaussPoints must be 2 or 3")
+    return xi, w
+
+
+def basis_function(xi, eta=None, zeta=None, FunctionClass="Q1"):
+    """Shape functions and reference gradients (src/fem.jl:48-114).
+
+    Returns ``(N, dN)``; ``dN`` is (nen, ndim) with column k = dN/dxi_k, or
+    the 1x2 row of the reference in 1D.
+    """
+    ndim = 3 if zeta is not None else (2 if eta is not None else 1)
+    fc = {"Q1": L.Q1, "Q2": L.Q2}.get(FunctionClass)
+    if fc is None:
+        raise SfemError(L.SFEM_BAD_ARG, "FunctionClass must be 'Q1' or 'Q2'")
+    nen = 9 if fc == L.Q2 else 2 ** ndim
+    N = np.zeros(nen)
+    dN = np.zeros(nen * ndim)
+    code = lib().sfem_basis_function(ndim, fc, float(xi), float(eta or 0.0), float(zeta or 0.0),
+                                     N.ctypes.data, dN.ctypes.data)
+    if code != L.SFEM_OK:
+        raise SfemError(code, f"basis_function: {FunctionClass} is not defined in {ndim}D")
+    if ndim == 1:
+        return N, dN.reshape(1, 2)
+    return N, dN.reshape(ndim, nen).T.copy()
+
+
+# ---------------------------------------------------------------------------
+# mesh / matrix handles
+# ---------------------------------------------------------------------------
+
+class Mesh:
+    """A mesh uploaded to the GPU (sfem_mesh_create) and its sparsity pattern."""
+
+    def __init__(self, ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1, ID=None, ctx=None,
+                 nNodes=None, nen=None, ldIEN=None):
+        self.ctx = ctx or get_context()
+        self.ndim = int(ndim)
+        self.nDof = int(nDof)
+        self.ne = int(ne)
+        fc = {"Q1": L.Q1, "Q2": L.Q2}.get(FunctionClass)
+        if fc is None:
+            raise SfemError(L.SFEM_BAD_ARG, "FunctionClass must be 'Q1' or 'Q2'")
+        X = _Buf(NodeList, np.float64)
+        E = _Buf(IEN, np.int64)
+        I = _Buf(ID, np.int64) if nDof > 1 else _Buf(None, np.int64)
+        space = _space(X, E, I)
+        if nNodes is None:
+            nNodes = np.shape(NodeList)[1]
+        if ldIEN is None or nen is None:
+            rows, cols = np.shape(IEN)[0], np.shape(IEN)[1]
+            ldIEN = rows if ldIEN is None else ldIEN
+            nen = cols if nen is None else nen
+        self.nNodes = int(nNodes)
+        h = C.c_void_p()
+        code = lib().sfem_mesh_create(self.ctx.h, self.ndim, fc, self.nDof, self.ne, X.ptr,
+                                      self.nNodes, E.ptr, int(ldIEN), int(nen), I.ptr, space,
+                                      C.byref(h))
+        check(code, self.ctx.h)
+        self.h = h
+
+    def pattern(self):
+        n, nnz = C.c_int64(), C.c_int64()
+        check(lib().sfem_pattern_build(self.ctx.h, self.h, C.byref(n), C.byref(nnz)), self.ctx.h)
+        return n.value, nnz.value
+
+    def assemble(self, Young=1, nu=0.3, plane="stress"):
+        Y = _Buf(np.atleast_1d(Young) if not _is_dev(Young) else Young, np.float64)
+        V = _Buf(np.atleast_1d(nu) if not _is_dev(nu) else nu, np.float64)
+        h = C.c_void_p()
+        code = lib().sfem_assemble(self.ctx.h, self.h, _plane(plane), Y.ptr, Y.size, V.ptr,
+                                   V.size, _space(Y, V), C.byref(h))
+        check(code, self.ctx.h)
+        return Matrix(self.ctx, h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sfem_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _plane(plane):
+    if plane in ("stress", L.PLANE_STRESS):
+        return L.PLANE_STRESS
+    if plane in ("strain", L.PLANE_STRAIN):
+        return L.PLANE_STRAIN
+    raise SfemError(L.SFEM_BAD_ARG, "plane must be 'stress' or 'strain'")
+
+
+class Matrix:
+    """Assembled K resident on the GPU (sfem_matrix)."""
+
+    def __init__(self, ctx, h):
+        self.ctx = ctx
+        self.h = h
+        n, nnz = C.c_int64(), C.c_int64()
+        check(lib().sfem_matrix_info(h, C.byref(n), C.byref(nnz)), ctx.h)
+        self.n, self.nnz = n.value, nnz.value
+
+    @property
+    def shape(self):
+        return (self.n, self.n)
+
+    def to_csc_arrays(self):
+        """(colptr, rowval, nzval), 1-based -- SparseMatrixCSC's fields."""
+        colptr = np.empty(self.n + 1, np.int64)
+        rowval = np.empty(self.nnz, np.int64)
+        nzval = np.empty(self.nnz, np.float64)
+        check(lib().sfem_matrix_export_csc(self.ctx.h, self.h, colptr.ctypes.data,
+                                           rowval.ctypes.data if self.nnz else None,
+                                           nzval.ctypes.data if self.nnz else None, L.MEM_HOST),
+              self.ctx.h)
+        return colptr, rowval, nzval
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        colptr, rowval, nzval = self.to_csc_arrays()
+        return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=self.shape)
+
+    def solve(self, fixed_dofs, fixed_vals, f=None, precision="fp64", precond="jacobi",
+              rtol=1e-10, maxit=100000, check_every=32, reliable_delta=0.1, profile=False,
+              out=None):
+        """Dirichlet solve (examples/vector3D.jl:314-322); returns ``(u, stats)``.
+
+        ``fixed_dofs`` are 1-based global DOF ids.  ``out`` may be a device
+        tensor (then every array argument must be on the device).
+        """
+        opts = L.SolveOpts()
+        lib().sfem_solve_opts_default(C.byref(opts))
+        opts.precision = {"fp64": L.FP64, "mixed": L.MIXED}[precision]
+        opts.precond = {"jacobi": L.PC_JACOBI, "block_jacobi": L.PC_BLOCK_JACOBI}[precond]
+        opts.rtol = rtol
+        opts.maxit = maxit
+        opts.check_every = check_every
+        opts.reliable_delta = reliable_delta
+        opts.profile = 1 if profile else 0
+        Fd = _Buf(fixed_dofs, np.int64)
+        Fv = _Buf(fixed_vals, np.float64)
+        Ff = _Buf(f, np.float64)
+        if out is None:
+            if _space(Fd, Fv, Ff) == L.MEM_DEVICE:
+                out = _torch.empty(self.n, dtype=_torch.float64, device=Fd.keep.device)
+            else:
+                out = np.empty(self.n)
+        U = _Buf.__new__(_Buf)
+        if _is_dev(out):
+            U.keep, U.ptr, U.space, U.size = out, C.c_void_p(out.data_ptr()), L.MEM_DEVICE, out.numel()
+        else:
+            U.keep, U.ptr, U.space, U.size = out, C.c_void_p(out.ctypes.data), L.MEM_HOST, out.size
+        space = _space(Fd, Fv, Ff, U)
+        stats = L.SolveStats()
+        code = lib().sfem_solve_dirichlet(self.ctx.h, self.h, Fd.ptr, Fd.size if Fd.ptr else 0,
+                                          Fv.ptr, Ff.ptr, U.ptr, space, C.byref(opts),
+                                          C.byref(stats))
+        check(code, self.ctx.h)
+        return out, stats.as_dict()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sfem_matrix_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# reference-shaped entry points
+# ---------------------------------------------------------------------------
+
+def assemble_system(ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1, ID=None, Young=1,
+                    nu=0.3, plane="stress", ctx=None, as_handle=False):
+    """``assemble_system`` of src/fem.jl:135-256 on the GPU.
+
+    Processes elements ``1:ne^ndim`` of ``IEN`` (src/fem.jl:179).  Returns the
+    stiffness matrix as ``scipy.sparse.csc_matrix`` -- same size, pattern and
+    values (to rounding) as ``sparse(E,J,V)`` at src/fem.jl:253 -- or the GPU
+    :class:`Matrix` handle when ``as_handle`` is true.  ``Young``/``nu`` may
+    be scalars (the reference) or per-element arrays; ``plane`` picks the 2D
+    law (the reference's is plane stress).
+    """
+    ctx = ctx or get_context()
+    fc = {"Q1": L.Q1, "Q2": L.Q2}.get(FunctionClass)
+    if fc is None:
+        raise SfemError(L.SFEM_BAD_ARG, "FunctionClass must be 'Q1' or 'Q2'")
+    X = _Buf(NodeList, np.float64)
+    E = _Buf(IEN, np.int64)
+    I = _Buf(ID, np.int64) if int(nDof) > 1 else _Buf(None, np.int64)
+    Y = _Buf(np.atleast_1d(Young) if not _is_dev(Young) else Young, np.float64)
+    V = _Buf(np.atleast_1d(nu) if not _is_dev(nu) else nu, np.float64)
+    space = _space(X, E, I, Y, V)
+    rows, cols = np.shape(IEN)[0], np.shape(IEN)[1]
+    h = C.c_void_p()
+    n, nnz = C.c_int64(), C.c_int64()
+    code = lib().sfem_assemble_system(ctx.h, int(ne), X.ptr, int(np.shape(NodeList)[1]), E.ptr,
+                                      int(rows), int(cols), int(ndim), fc, int(nDof), I.ptr, Y.ptr,
+                                      Y.size, V.ptr, V.size, _plane(plane), space, C.byref(h),
+                                      C.byref(n), C.byref(nnz))
+    check(code, ctx.h)
+    K = Matrix(ctx, h)
+    if as_handle:
+        return K
+    try:
+        return K.to_scipy()
+    finally:
+        K.close()
+
+
+def solve_dirichlet(K, fixed_dofs, fixed_vals, f=None, **opts):
+    """``q = q_d + C * (K_free \\ C'(f - K q_d))`` (examples/vector3D.jl:314-322).
+
+    ``K`` is a :class:`Matrix` handle from ``assemble_system(...,
+    as_handle=True)``.  Returns ``(q, stats)``.
+    """
+    if not isinstance(K, Matrix):
+        raise SfemError(L.SFEM_BAD_ARG, "solve_dirichlet needs the GPU matrix handle "
+                                        "(assemble_system(..., as_handle=True))")
+    return K.solve(fixed_dofs, fixed_vals, f, **opts)
