@@ -1,0 +1,423 @@
+"""Benchmark: solved DOF/s of the smearFEM.jl hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--ne 128]
+
+Workload (one "step"): the 128^3 Q1 hex elasticity problem -- 2,146,689 nodes,
+6,440,067 DOFs, 513,599,625 nonzeros -- with seeded interior jitter 0.2h,
+per-element E ~ lognormal(0, 0.5), nu = 0.3, bottom face clamped and a
+seeded 4-mode z-displacement on the top face.  A step is the whole path:
+mesh upload/validation, device sparsity pattern, FP64 element stiffness and
+assembly, Dirichlet elimination and Jacobi-PCG to 1e-10 relative residual.
+
+  value     DOF / step time, inputs already resident in HBM (FP64 path)
+  mixed     the same step with the FP32-inner / FP64-refresh solver
+  e2e       the same metric through the C ABI with host buffers: pinned
+            host -> device copies of every input and the device -> host copy
+            of u inside the timed region
+  roofline  the FP64 SpMV (the dominant kernel): algorithmic bytes per launch
+            over its CUDA-event launch time, against MEASURED_PEAKS.json
+  cpu_baseline  the C restatement of the reference (oracle/sfem_oracle.c) on
+            the host cores, timed on a bounded sample and scaled (see
+            ``cpu_sample``)
+
+With N > 1 (torchrun) every rank solves its own replica on its own GPU
+("replicas only": the path has no exchange step); value sums all ranks'
+DOFs over the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import __graft_entry__ as GE  # noqa: E402
+
+METRIC = "solved DOF/s at 1e-8 rel. error (mixed vs plain FP64); served p50/p99 latency"
+UNIT = "DOF/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ne", type=int, default=128)
+    ap.add_argument("--rtol", type=float, default=1e-10)
+    ap.add_argument("--no-extras", action="store_true", help="value only (no mixed/e2e/cpu legs)")
+    return ap.parse_args(argv)
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas; barrier + max over ranks only)
+# ---------------------------------------------------------------------------
+
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", 0))
+        self.world = int(os.environ.get("WORLD_SIZE", 1))
+        self.local = int(os.environ.get("LOCAL_RANK", 0))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def aggregate(dist, units_per_rank, ms_per_rank):
+    """Whole-job throughput: all ranks' units over the slowest rank's time."""
+    ms = dist.max(ms_per_rank)
+    units = units_per_rank * dist.world
+    return units / (ms * 1e-3), ms
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+        sm = np.array([num(r[1]) for r in rows])
+        mx = np.nanmax([num(r[2]) for r in rows])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        loaded = sm[sm > 0.5 * mx] if np.isfinite(mx) else sm
+        return {"sm_mhz": float(np.nanmedian(loaded if loaded.size else sm)), "sm_max_mhz": float(mx),
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": float(np.nanmax([num(r[3]) for r in rows]))}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def probe_fp64_peak(device):
+    import ctypes
+    path = os.path.join(GE.PKG_DIR, "lib", "libsfem_probe.so")
+    if not os.path.exists(path):
+        return None, None
+    L = ctypes.CDLL(path)
+    t64, t32 = ctypes.c_double(), ctypes.c_double()
+    ok = L.sfem_probe_fp64_tflops(device, ctypes.byref(t64)) == 0
+    ok &= L.sfem_probe_fp32_tflops(device, ctypes.byref(t32)) == 0
+    return (t64.value, t32.value) if ok else (None, None)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the C restatement of the reference, bounded sample
+# ---------------------------------------------------------------------------
+
+def cpu_sample(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=64, sample_iters=40):
+    """Time the oracle's assembly of the ``sample_ne``^3 instance of the same
+    generator (element loop + COO->CSC, scaled by the element-count ratio)
+    and ``sample_iters`` of its Jacobi-PCG iterations (scaled by the nnz ratio
+    and by ``iters_full``, the iteration count of the full-size solve).
+    Returns (DOF/s estimate for the full workload, details)."""
+    from oracle import coracle
+    coracle.build()
+    threads = coracle.max_threads()
+    q = pkg.meshgen.config2(ne=sample_ne)
+    t0 = time.perf_counter()
+    K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3, nthreads=threads)
+    t_asm = time.perf_counter() - t0
+    _, st1 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=1, nthreads=threads)
+    _, st2 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=sample_iters + 1, nthreads=threads)
+    t_iter = max(1e-9, (st2["seconds"] - st1["seconds"]) / sample_iters)
+    _, _, nzs, _, n_s = K.arrays()
+    nnz_s = len(nzs)
+    del K
+    scale_el = (ne_full / sample_ne) ** 3
+    t_full = t_asm * scale_el + t_iter * (nnz_full / nnz_s) * iters_full
+    return n_dof_full / t_full, {
+        "cores": threads, "t_assemble_sample_s": t_asm, "t_iter_sample_s": t_iter,
+        "est_full_s": t_full,
+        "sample": (f"oracle assembly (element loop + COO->CSC) of the {sample_ne}^3 instance of the same "
+                   f"generator scaled x{scale_el:.0f} by element count, plus {sample_iters} of its "
+                   f"Jacobi-PCG iterations scaled by nnz ({nnz_full}/{nnz_s}) and by the "
+                   f"{iters_full} iterations the full {ne_full}^3 solve takes")}
+
+
+def reference_arm(args, dist):
+    """--impl reference: the reference's algorithm on the host cores (oracle port)."""
+    if dist.rank != 0:
+        return 0
+    pkg = GE.load_package()
+    ne = args.ne
+    n_dof = 3 * (ne + 1) ** 3
+    nnz = 9 * (3 * (ne + 1) - 2) ** 3
+    # Iteration count of the full-size Jacobi-PCG: from the full solve of the
+    # sample instance, scaled linearly in ne (Jacobi-PCG on Q1 elasticity:
+    # sqrt(cond) ~ 1/h).
+    from oracle import coracle
+    coracle.build()
+    sample_ne = min(64, ne)
+    q = pkg.meshgen.config2(ne=sample_ne)
+    Kq = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3,
+                          nthreads=coracle.max_threads())
+    _, st = Kq.solve(q.fixed_dofs, q.fixed_vals, rtol=args.rtol, nthreads=coracle.max_threads())
+    del Kq
+    iters_full = int(round(st["iters"] * ne / sample_ne))
+    vals = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        v, det = cpu_sample(pkg, ne, n_dof, nnz, iters_full, sample_ne=sample_ne)
+        if k >= args.warmup:
+            vals.append((v, time.perf_counter() - t0, det))
+    value = float(np.median([v for v, _, _ in vals]))
+    det = vals[-1][2]
+    line = {
+        "metric": METRIC, "impl": "reference", "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean([t for _, t, _ in vals]) * 1e3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded jittered Q1 hex mesh, E ~ lognormal(0, 0.5), 4-mode top displacement",
+        "config": {"workload": f"{ne}^3 Q1 hex elasticity, FP64 assembly + Jacobi-PCG to {args.rtol:g}",
+                   "ne": ne, "n_dof": n_dof, "nnz": nnz,
+                   "iterations_full_estimate": iters_full,
+                   "iterations_sample_full_solve": st["iters"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": det["cores"], "kind": "port",
+                         "sample": det["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def our_arm(args, dist):
+    import torch
+
+    pkg = GE.load_package()
+    dev_index = dist.local
+    torch.cuda.set_device(dev_index)
+    dev = torch.device("cuda", dev_index)
+    ctx = pkg.get_context(dev_index)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    p = pkg.meshgen.config2(ne=args.ne)
+    nN, nEl = p.n_nodes, p.n_elem
+    n_dof = p.n_dof
+    NLf = np.asfortranarray(p.NodeList)
+    IENf = np.asfortranarray(p.IEN)
+    IDf = np.asfortranarray(p.ID)
+    # device-resident inputs in the reference's (column-major) memory order
+    dX = torch.from_numpy(NLf.ravel(order="F")).to(dev)
+    dIEN = torch.from_numpy(IENf.ravel(order="F")).to(dev)
+    dID = torch.from_numpy(IDf.ravel(order="F")).to(dev)
+    dY = torch.from_numpy(p.Young).to(dev)
+    dNU = torch.tensor([0.3], dtype=torch.float64, device=dev)
+    dFD = torch.from_numpy(p.fixed_dofs).to(dev)
+    dFV = torch.from_numpy(p.fixed_vals).to(dev)
+    dU = torch.empty(n_dof, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+
+    def step(precision="fp64", precond="jacobi", rtol=args.rtol, profile=False, out=dU):
+        t0 = time.perf_counter()
+        m = pkg.Mesh(p.ne, dX, dIEN, 3, "Q1", 3, dID, ctx=ctx, nNodes=nN, nen=8, ldIEN=nEl)
+        K = m.assemble(dY, dNU)
+        t1 = time.perf_counter()
+        _, st = K.solve(dFD, dFV, precision=precision, precond=precond, rtol=rtol, profile=profile,
+                        out=out)
+        t2 = time.perf_counter()
+        info = dict(st, n=K.n, nnz=K.nnz, asm_s=t1 - t0, solve_s=t2 - t1)
+        K.close()
+        m.close()
+        return info
+
+    def timed(fn, k, w):
+        for _ in range(w):
+            fn()
+        dist.barrier()
+        torch.cuda.synchronize()
+        ctx.sync()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        launches0 = ctx.kernel_launches()
+        e0.record(stream)
+        infos = [fn() for _ in range(k)]
+        e1.record(stream)
+        e1.synchronize()
+        ctx.sync()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        dist.barrier()
+        return ms, infos, ctx.kernel_launches() - launches0
+
+    # reference displacement for the error report: FP64 Jacobi-PCG to 1e-13 (untimed)
+    uref = torch.empty_like(dU)
+    ref_info = step(rtol=1e-13, out=uref)
+    uref_h = uref.cpu().numpy()
+
+    def rel_err(u):
+        return float(np.linalg.norm(u.cpu().numpy() - uref_h) / np.linalg.norm(uref_h))
+
+    # ---- value: FP64 path, device-resident inputs, SpMV launches event-timed
+    clocks = ClockSampler(dev_index)
+    clocks.start()
+    ms, infos, launches = timed(lambda: step(profile=True), args.steps, args.warmup)
+    clk = clocks.stop()
+    it = infos[-1]["iterations"]
+    err64 = rel_err(dU)
+    value, ms = aggregate(dist, n_dof, ms)
+    spmv_ms = sum(i["ms_spmv"] for i in infos) / max(1, sum(i["spmv_launches"] for i in infos))
+    nnz = infos[-1]["nnz"]
+    nnzb = nnz // 9
+    nd = 3 * nN
+    spmv_bytes = nnz * 8 + nnzb * 4 + nd * 8 * 2 + nd
+    hbm_peak, peak_kind = measured_peaks()
+    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    fp64_peak, fp32_peak = probe_fp64_peak(dev_index)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded jittered Q1 hex mesh, E ~ lognormal(0, 0.5), 4-mode top displacement",
+        "config": {"workload": f"{args.ne}^3 Q1 hex elasticity (configs[1]): FP64 assembly + "
+                               f"Jacobi-PCG to {args.rtol:g}",
+                   "ne": args.ne, "n_dof": n_dof, "nnz": nnz, "precision": "fp64", "precond": "jacobi",
+                   "rtol": args.rtol, "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2 (K alone is %.1f GB), no flush" % (nnz * 8 / 1e9)},
+        "iterations": it, "relres": infos[-1]["relres"], "rel_err": err64,
+        "rel_err_reference": "FP64 Jacobi-PCG on the GPU to relative residual 1e-13",
+        "breakdown_s": {"upload_pattern_assemble": float(np.mean([i["asm_s"] for i in infos])),
+                        "dirichlet_solve": float(np.mean([i["solve_s"] for i in infos]))},
+        "roofline": {"kernel": "k_spmv<double,3> (masked sliced-ELL 3x3-block SpMV, fused p.Ap)",
+                     "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": spmv_bytes, "launch_ms": spmv_ms,
+                     "traffic": None},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if fp64_peak:
+        fl = 2.0 * nnz / (spmv_ms * 1e-3) / 1e12
+        line["fp64_pipe"] = {"spmv_tflops": fl, "probe_fp64_tflops": fp64_peak, "frac": fl / fp64_peak,
+                             "probe_fp32_tflops": fp32_peak}
+    if not args.no_extras:
+        # ---- mixed precision on the same workload
+        msm, infm, _ = timed(lambda: step(precision="mixed", precond="block_jacobi", profile=True),
+                             args.steps, args.warmup)
+        vmix, msm = aggregate(dist, n_dof, msm)
+        line["mixed"] = {"value": vmix, "ms_per_step": msm,
+                         "precond": "block_jacobi", "iterations": infm[-1]["iterations"],
+                         "fp64_refreshes": infm[-1]["reliable_updates"], "relres": infm[-1]["relres"],
+                         "rel_err": rel_err(dU), "speedup_vs_fp64": ms / msm,
+                         "spmv32_ms": sum(i["ms_spmv"] for i in infm) / max(1, sum(i["spmv_launches"] for i in infm))}
+        # ---- e2e: C ABI with pinned host buffers, copies inside the timed region
+        def pinned(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            return t.numpy()
+        hX = pinned(NLf.ravel(order="F")).reshape(NLf.shape, order="F")
+        hIEN = pinned(IENf.ravel(order="F")).reshape(IENf.shape, order="F")
+        hID = pinned(IDf.ravel(order="F")).reshape(IDf.shape, order="F")
+        hY, hFD, hFV = pinned(p.Young), pinned(p.fixed_dofs), pinned(p.fixed_vals)
+        hU = torch.empty(n_dof, dtype=torch.float64).pin_memory().numpy()
+
+        def step_e2e():
+            K = pkg.assemble_system(p.ne, hX, hIEN, 3, "Q1", 3, hID, hY, 0.3, ctx=ctx, as_handle=True)
+            K.solve(hFD, hFV, rtol=args.rtol, out=hU)
+            K.close()
+        mse, _, _ = timed(step_e2e, args.steps, min(args.warmup, 1))
+        ve2e, mse = aggregate(dist, n_dof, mse)
+        h2d = hX.nbytes + hIEN.nbytes + hID.nbytes + hY.nbytes + 8 + hFD.nbytes + hFV.nbytes
+        line["e2e"] = {"value": ve2e, "unit": UNIT, "ms_per_step": mse,
+                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hU.nbytes),
+                       "rel_err": float(np.linalg.norm(hU - uref_h) / np.linalg.norm(uref_h))}
+        # ---- CPU baseline (rank 0, N=1 only)
+        if dist.world == 1:
+            v, det = cpu_sample(pkg, args.ne, n_dof, nnz, it)
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",
+                                    "sample": det["sample"]}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return reference_arm(args, dist)
+        return our_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

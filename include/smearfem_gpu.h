@@ -80,6 +80,11 @@ SFEM_API const char *sfem_last_error(const sfem_ctx *ctx);
 SFEM_API int sfem_ctx_synchronize(sfem_ctx *ctx);
 /* Library version string. */
 SFEM_API const char *sfem_version(void);
+/* The context's CUDA stream (a cudaStream_t), so callers can order their own
+ * work and CUDA events against the library's (no reference counterpart). */
+SFEM_API void *sfem_ctx_stream(sfem_ctx *ctx);
+/* Kernels the context has launched so far (graph-launched kernels included). */
+SFEM_API int64_t sfem_ctx_kernel_launches(const sfem_ctx *ctx);
 
 /* ---- host helpers (pure host code, identical expressions) --------------- */
 

@@ -61,6 +61,8 @@ SIGNATURES = {
     "sfem_last_error": (C.c_char_p, [P]),
     "sfem_ctx_synchronize": (C.c_int, [P]),
     "sfem_version": (C.c_char_p, []),
+    "sfem_ctx_stream": (C.c_void_p, [P]),
+    "sfem_ctx_kernel_launches": (C.c_int64, [P]),
     "sfem_gaussian_quadrature": (C.c_int, [C.c_double, C.c_double, C.c_int, P, P]),
     "sfem_basis_function": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, P, P]),
     "sfem_mesh_create": (C.c_int, [P, C.c_int, C.c_int, C.c_int, I64, P, I64, P, I64, C.c_int, P,

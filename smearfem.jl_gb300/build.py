@@ -23,6 +23,8 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(OUT_DIR, "libsmearfem_gpu.so")
+PROBE_SRC = os.path.join(PKG, "probe", "peaks.cu")
+PROBE_LIB = os.path.join(OUT_DIR, "libsfem_probe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fvisibility=hidden"]
@@ -73,6 +75,13 @@ def build(force=False, verbose=False, extra_flags=()):
         if p.returncode != 0:
             raise RuntimeError(f"link failed:\n{p.stderr}")
         os.replace(tmp, LIB)
+    if force or _stale(PROBE_LIB, [PROBE_SRC]):
+        tmp = PROBE_LIB + f".{os.getpid()}.tmp"
+        cmd = [exe, *ARCH, *NVCC_FLAGS, "-shared", "-o", tmp, PROBE_SRC]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"probe build failed:\n{p.stderr}")
+        os.replace(tmp, PROBE_LIB)
     return LIB
 
 

@@ -272,6 +272,10 @@ extern "C" int sfem_ctx_synchronize(sfem_ctx *ctx) {
 
 extern "C" const char *sfem_version(void) { return SFEM_VERSION; }
 
+extern "C" void *sfem_ctx_stream(sfem_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" int64_t sfem_ctx_kernel_launches(const sfem_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
 // ---------------------------------------------------------------------------
 // C ABI: host helpers, src/fem.jl:21-31 and :48-114 (same expressions)
 // ---------------------------------------------------------------------------

@@ -42,8 +42,11 @@ constexpr int SPMV_T = 256;
 constexpr int UPD_T = 256;
 
 struct CgScalars {
-    double rz, rz_prev, pAp, alpha, beta, rr, bb, tol2, rr_ref;
+    double rz, rz_prev, pAp, alpha, beta, rr, bb, tol2, rr_ref, delta2;
     int it, done, status, maxit;
+    int refresh;      // mixed: FP64 residual refresh requested by k_update
+    int maxit_hit;    // mixed: stop after the pending refresh
+    int nrefresh;     // mixed: refreshes performed
     unsigned int ticket[4];
 };
 
@@ -108,13 +111,15 @@ __device__ bool reduce2_last(double a, double b, double *partial, unsigned int *
     return true;
 }
 
-// y = mask .* (K x); MODE 1 additionally reduces x.y into pAp and sets alpha.
+// y = mask .* (K x); MODE 1 additionally reduces x.y into pAp and sets alpha;
+// MODE 2 runs only while a mixed-precision refresh is pending.
 template <typename T, int B, int MODE>
 __global__ void __launch_bounds__(SPMV_T)
 k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val, int64_t nN,
        int64_t nslices, const T *__restrict__ x, T *__restrict__ y, const unsigned char *__restrict__ fixed,
        CgScalars *S, double *partial) {
     if (MODE == 1 && S->done) return;
+    if (MODE == 2 && !S->refresh) return;
     const int lane = threadIdx.x & 31;
     const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     double dot = 0.0;
@@ -169,7 +174,10 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
 
 // x += alpha p; r -= alpha q; z = M^-1 r; reduce r.z and r.r; CG scalar update.
 // PC: 0 Jacobi (minv per DOF), 1 block-Jacobi (minv: B x B per node).
-template <typename T, int B, int PC>
+// MIXED: the recursive FP32 residual never ends the solve; reaching the
+// tolerance, dropping by delta since the last refresh, or hitting maxit
+// requests an FP64 refresh instead (k_fold / k_spmv MODE 2 / k_refresh).
+template <typename T, int B, int PC, bool MIXED>
 __global__ void __launch_bounds__(UPD_T)
 k_update(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
          const T *__restrict__ q, const T *__restrict__ minv, CgScalars *S, double *partial) {
@@ -208,15 +216,18 @@ k_update(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, co
         S->rz_prev = S->rz;
         S->rz = trz;
         S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
-        if (trr <= S->tol2) {
+        if (!(trr == trr)) {
+            S->done = 1;
+            S->status = SFEM_SINGULAR;
+        } else if (MIXED) {
+            if (S->it >= S->maxit) S->maxit_hit = 1;
+            if (trr <= S->tol2 || trr <= S->delta2 * S->rr_ref || S->maxit_hit) S->refresh = 1;
+        } else if (trr <= S->tol2) {
             S->done = 1;
             S->status = SFEM_OK;
         } else if (S->it >= S->maxit) {
             S->done = 1;
             S->status = SFEM_NOT_CONVERGED;
-        } else if (!(trr == trr)) {
-            S->done = 1;
-            S->status = SFEM_SINGULAR;
         }
     }
 }
@@ -376,7 +387,8 @@ __global__ void k_cast(int64_t n, const double *__restrict__ a, T *__restrict__ 
     if (i < n) b[i] = (T)a[i];
 }
 
-__global__ void k_fold(int64_t n, double *__restrict__ x64, float *__restrict__ x32) {
+__global__ void k_fold(int64_t n, double *__restrict__ x64, float *__restrict__ x32, const CgScalars *S) {
+    if (!S->refresh) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     x64[i] += (double)x32[i];
@@ -389,6 +401,7 @@ __global__ void __launch_bounds__(UPD_T)
 k_refresh(int64_t nN, const double *__restrict__ bvec, const double *__restrict__ Kx, const unsigned char *__restrict__ fixed,
           double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ z32, const float *__restrict__ minv,
           CgScalars *S, double *partial) {
+    if (!S->refresh) return;
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double rz = 0.0, rr = 0.0;
     if (node < nN) {
@@ -422,11 +435,13 @@ k_refresh(int64_t nN, const double *__restrict__ bvec, const double *__restrict_
         S->rr_ref = trr;
         S->rz = trz;
         S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        S->refresh = 0;
+        S->nrefresh += 1;
         if (trr <= S->tol2) {
             S->done = 1;
             S->status = SFEM_OK;
-        } else {
-            S->done = 0;
+        } else if (S->maxit_hit) {
+            S->done = 1;
             S->status = SFEM_NOT_CONVERGED;
         }
     }
@@ -512,8 +527,8 @@ class Solver {
     }
     template <int B>
     int solve_b(double *x64_out);
-    template <typename T, int B, int PC>
-    int cg_loop(Vecs<T> &v, bool mixed, double *x64, double *r64, double *q64);
+    template <typename T, int B, int PC, bool MIXED>
+    int cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64);
     template <typename T, int B>
     void launch_spmv(const T *val, const T *x, T *y, bool fused);
     int read_scalars(CgScalars *h);
@@ -555,8 +570,8 @@ int Solver::read_scalars(CgScalars *h) {
     return SFEM_OK;
 }
 
-template <typename T, int B, int PC>
-int Solver::cg_loop(Vecs<T> &v, bool mixed, double *x64, double *r64, double *q64) {
+template <typename T, int B, int PC, bool MIXED>
+int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
     const T *val = nullptr;
     if constexpr (sizeof(T) == 8) val = (const T *)K->val;
     else val = (const T *)K->val32;
@@ -569,9 +584,20 @@ int Solver::cg_loop(Vecs<T> &v, bool mixed, double *x64, double *r64, double *q6
         if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
         launch_spmv<T, B>(val, v.p, v.q, true);
         if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
-        k_update<T, B, PC><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.x, v.r, v.z, v.p, v.q, v.minv, S, partial);
+        k_update<T, B, PC, MIXED><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.x, v.r, v.z, v.p, v.q, v.minv, S,
+                                                                       partial);
         SFEM_LAUNCHED(ctx);
+        if constexpr (MIXED) {
+            // FP64 refresh, skipped on the device unless k_update requested it
+            k_fold<<<vec_grid, 256, 0, ctx->stream>>>(nd, x64, (float *)v.x, S);
+            k_spmv<double, B, 2><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(m->sliceptr, m->col, K->val, m->nN,
+                                                                       m->nslices, x64, q64, fixed, S, partial);
+            k_refresh<B, PC><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, bvec, q64, fixed, r64, (float *)v.r,
+                                                                  (float *)v.z, (const float *)v.minv, S, partial);
+            ctx->launches += 3;
+        }
     };
+    const int per_iter = MIXED ? 6 : 3;
     if (profile) {
         events.resize(2 * chunk);
         for (auto &e : events) SFEM_CUDA(ctx, cudaEventCreate(&e));
@@ -587,14 +613,12 @@ int Solver::cg_loop(Vecs<T> &v, bool mixed, double *x64, double *r64, double *q6
         ctx->launches = before;  // counted per graph launch below
     }
     int it_prev = 0;
-    const double delta2 = opts.reliable_delta * opts.reliable_delta;
-    int guard = 0;
     while (true) {
         if (profile) {
             for (int i = 0; i < chunk; ++i) enqueue_iter(i);
         } else {
             SFEM_CUDA(ctx, cudaGraphLaunch(gexec, ctx->stream));
-            ctx->launches += 3 * chunk;
+            ctx->launches += (long long)per_iter * chunk;
         }
         SFEM_TRY(read_scalars(h));
         if (profile) {
@@ -608,33 +632,10 @@ int Solver::cg_loop(Vecs<T> &v, bool mixed, double *x64, double *r64, double *q6
                 }
             }
         }
-        if (mixed) {
-            const bool conv = h->done && h->status == SFEM_OK;
-            const bool drop = h->rr <= delta2 * h->rr_ref;
-            if ((conv || drop || (h->done && h->status == SFEM_NOT_CONVERGED && h->it >= h->maxit)) &&
-                h->status != SFEM_SINGULAR) {
-                // FP64 refresh: x64 += x32, r = b - K x64, restart the recurrences from it
-                k_fold<<<vec_grid, 256, 0, ctx->stream>>>(nd, x64, (float *)v.x);
-                SFEM_LAUNCHED(ctx);
-                launch_spmv<double, B>(K->val, x64, q64, false);
-                k_refresh<B, PC><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, bvec, q64, fixed, r64, (float *)v.r,
-                                                                      (float *)v.z, (const float *)v.minv, S, partial);
-                SFEM_LAUNCHED(ctx);
-                reliable++;
-                SFEM_TRY(read_scalars(h));
-                it_prev = h->it;
-                if (h->done && h->status == SFEM_OK) break;
-                if (h->it >= h->maxit) {
-                    h->status = SFEM_NOT_CONVERGED;
-                    break;
-                }
-                continue;
-            }
-        }
-        if (h->done) break;
         it_prev = h->it;
-        if (++guard > (1 << 30)) break;
+        if (h->done) break;
     }
+    reliable = h->nrefresh;
     iterations = h->it;
     status = h->status;
     if constexpr (sizeof(T) == 8) {
@@ -681,8 +682,8 @@ int Solver::solve_b(double *x64) {
         else
             k_init<double, B, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
         SFEM_LAUNCHED(ctx);
-        SFEM_TRY(block ? cg_loop<double, B, 1>(v, false, nullptr, nullptr, nullptr)
-                       : cg_loop<double, B, 0>(v, false, nullptr, nullptr, nullptr));
+        SFEM_TRY(block ? cg_loop<double, B, 1, false>(v, nullptr, nullptr, nullptr)
+                       : cg_loop<double, B, 0, false>(v, nullptr, nullptr, nullptr));
     } else {
         if (!K->val32) {
             const int64_t nv = m->nslabs * 32 * B * B;
@@ -711,7 +712,7 @@ int Solver::solve_b(double *x64) {
         else
             k_init<float, B, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
         SFEM_LAUNCHED(ctx);
-        SFEM_TRY(block ? cg_loop<float, B, 1>(v, true, x64, r64, q64) : cg_loop<float, B, 0>(v, true, x64, r64, q64));
+        SFEM_TRY(block ? cg_loop<float, B, 1, true>(v, x64, r64, q64) : cg_loop<float, B, 0, true>(v, x64, r64, q64));
     }
     return SFEM_OK;
 }
@@ -807,6 +808,7 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
     }
     hs.bb = bb;
     hs.tol2 = opts.rtol * opts.rtol * bb;
+    hs.delta2 = opts.reliable_delta * opts.reliable_delta;
     hs.rr = bb;
     hs.rr_ref = bb;
     hs.it = 0;

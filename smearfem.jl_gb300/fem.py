@@ -105,6 +105,14 @@ class Context:
     def error(self):
         return lib().sfem_last_error(self.h).decode()
 
+    @property
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        return lib().sfem_ctx_stream(self.h) or 0
+
+    def kernel_launches(self):
+        return int(lib().sfem_ctx_kernel_launches(self.h))
+
 
 _contexts = {}
 
