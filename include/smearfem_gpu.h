@@ -139,6 +139,36 @@ SFEM_API int sfem_assemble_system(sfem_ctx *ctx, int64_t ne, const double *NodeL
                          int64_t nYoung, const double *nu, int64_t nNu, int plane,
                          int mem_space, sfem_matrix **out, int64_t *n_out, int64_t *nnz_out);
 
+/* Re-assemble an existing matrix K for new Young/nu without allocating any
+ * device memory.  This entry point has no counterpart in the reference.
+ *
+ * It is meant for callers that cannot call cudaMalloc/cudaFree when they
+ * refresh K: processes whose device memory is owned by another allocator
+ * under a hard budget, latency-bound loops (load increments, material
+ * updates) in which cudaFree's device-wide synchronisation would stall other
+ * streams, and deployments that forbid dynamic allocation after start-up.
+ * Build the mesh, pattern and K once with the allocating calls above; this
+ * call then only launches kernels and copies into memory that already
+ * exists.  The result equals sfem_assemble with the same Young/nu.
+ *
+ *  - Scratch: a fixed 64 MiB device array (8,388,608 doubles) inside the
+ *    library, held on every GPU that loads it until the process exits.  It
+ *    must fit the element blocks (pairs*nDof^2 doubles per element: 324 for
+ *    a 3D elasticity hex, 40 for a 2D elasticity quad, 36 for a 3D Laplace
+ *    hex) plus the Young/nu values; larger meshes get SFEM_BAD_ARG.  That is
+ *    at most 25,890 hex elasticity elements with per-element Young.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) for that device; make that first call before any
+ *    stream capture.
+ *  - Every call, from any context, shares the one array: calls that overlap
+ *    on the GPU (other streams, other host threads) race.  Calls on one
+ *    context are ordered by its stream and do not.
+ *  - Young/nu: length 1 or ne^ndim, in `mem_space` (host or device).  The
+ *    FP32 copy of K used by SFEM_MIXED solves is refreshed too. */
+SFEM_API int sfem_reassemble_noalloc(sfem_ctx *ctx, sfem_matrix *K, const double *Young,
+                                     int64_t nYoung, const double *nu, int64_t nNu,
+                                     int mem_space);
+
 /* n = size(K,1) = size(K,2); nnz = length(nzval). */
 SFEM_API int sfem_matrix_info(const sfem_matrix *K, int64_t *n, int64_t *nnz);
 

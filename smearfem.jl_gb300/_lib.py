@@ -72,6 +72,7 @@ SIGNATURES = {
     "sfem_assemble": (C.c_int, [P, P, C.c_int, P, I64, P, I64, C.c_int, PP]),
     "sfem_assemble_system": (C.c_int, [P, I64, P, I64, P, I64, C.c_int, C.c_int, C.c_int, C.c_int,
                                        P, P, I64, P, I64, C.c_int, C.c_int, PP, I64P, I64P]),
+    "sfem_reassemble_noalloc": (C.c_int, [P, P, P, I64, P, I64, C.c_int]),
     "sfem_matrix_info": (C.c_int, [P, I64P, I64P]),
     "sfem_matrix_export_csc": (C.c_int, [P, P, P, P, P, C.c_int]),
     "sfem_matrix_destroy": (C.c_int, [P]),
