@@ -55,8 +55,12 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ne", type=int, default=128)
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--no-extras", action="store_true", help="value only (no mixed/e2e/cpu legs)")
-    return ap.parse_args(argv)
+    ap.add_argument("--legs", default="value,mixed,e2e,cpu",
+                    help="comma list of value,mixed,e2e,cpu (profiling runs pick one)")
+    ap.add_argument("--no-extras", action="store_true", help="same as --legs value")
+    a = ap.parse_args(argv)
+    a.legs = {"value"} if a.no_extras else set(x.strip() for x in a.legs.split(",") if x.strip())
+    return a
 
 
 # ---------------------------------------------------------------------------
@@ -327,57 +331,71 @@ def our_arm(args, dist):
         return float(np.linalg.norm(u.cpu().numpy() - uref_h) / np.linalg.norm(uref_h))
 
     # ---- value: FP64 path, device-resident inputs, SpMV launches event-timed
-    clocks = ClockSampler(dev_index)
-    clocks.start()
-    ms, infos, launches = timed(lambda: step(profile=True), args.steps, args.warmup)
-    clk = clocks.stop()
-    it = infos[-1]["iterations"]
-    err64 = rel_err(dU)
-    value, ms = aggregate(dist, n_dof, ms)
-    spmv_ms = sum(i["ms_spmv"] for i in infos) / max(1, sum(i["spmv_launches"] for i in infos))
-    nnz = infos[-1]["nnz"]
-    nnzb = nnz // 9
-    nd = 3 * nN
-    spmv_bytes = nnz * 8 + nnzb * 4 + nd * 8 * 2 + nd
-    hbm_peak, peak_kind = measured_peaks()
-    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
-    fp64_peak, fp32_peak = probe_fp64_peak(dev_index)
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: seeded jittered Q1 hex mesh, E ~ lognormal(0, 0.5), 4-mode top displacement",
-        "config": {"workload": f"{args.ne}^3 Q1 hex elasticity (configs[1]): FP64 assembly + "
-                               f"Jacobi-PCG to {args.rtol:g}",
-                   "ne": args.ne, "n_dof": n_dof, "nnz": nnz, "precision": "fp64", "precond": "jacobi",
-                   "rtol": args.rtol, "parallelism": f"replicas x{dist.world}",
-                   "l2": "inputs larger than L2 (K alone is %.1f GB), no flush" % (nnz * 8 / 1e9)},
-        "iterations": it, "relres": infos[-1]["relres"], "rel_err": err64,
-        "rel_err_reference": "FP64 Jacobi-PCG on the GPU to relative residual 1e-13",
-        "breakdown_s": {"upload_pattern_assemble": float(np.mean([i["asm_s"] for i in infos])),
-                        "dirichlet_solve": float(np.mean([i["solve_s"] for i in infos]))},
-        "roofline": {"kernel": "k_spmv<double,3> (masked sliced-ELL 3x3-block SpMV, fused p.Ap)",
-                     "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": spmv_bytes, "launch_ms": spmv_ms,
-                     "traffic": None},
-        "gpu_launches": int(launches),
-        "clocks": clk,
-    }
-    if fp64_peak:
-        fl = 2.0 * nnz / (spmv_ms * 1e-3) / 1e12
-        line["fp64_pipe"] = {"spmv_tflops": fl, "probe_fp64_tflops": fp64_peak, "frac": fl / fp64_peak,
-                             "probe_fp32_tflops": fp32_peak}
-    if not args.no_extras:
+    line = {"metric": METRIC, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic: seeded jittered Q1 hex mesh, E ~ lognormal(0, 0.5), 4-mode top displacement"}
+    it = ref_info["iterations"]
+    nnz = ref_info["nnz"]
+    if "value" in args.legs:
+        clocks = ClockSampler(dev_index)
+        clocks.start()
+        ms, infos, launches = timed(lambda: step(profile=True), args.steps, args.warmup)
+        clk = clocks.stop()
+        it = infos[-1]["iterations"]
+        err64 = rel_err(dU)
+        value, ms = aggregate(dist, n_dof, ms)
+        spmv_ms = sum(i["ms_spmv"] for i in infos) / max(1, sum(i["spmv_launches"] for i in infos))
+        nnzb = nnz // 9
+        nd = 3 * nN
+        spmv_bytes = nnz * 8 + nnzb * 4 + nd * 8 * 2 + nd
+        hbm_peak, peak_kind = measured_peaks()
+        achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+        fp64_peak, fp32_peak = probe_fp64_peak(dev_index)
+        line.update({
+            "value": value, "ms_per_step": ms,
+            "config": {"workload": f"{args.ne}^3 Q1 hex elasticity (configs[1]): FP64 assembly + "
+                                   f"Jacobi-PCG to {args.rtol:g}",
+                       "ne": args.ne, "n_dof": n_dof, "nnz": nnz, "precision": "fp64", "precond": "jacobi",
+                       "rtol": args.rtol, "parallelism": f"replicas x{dist.world}",
+                       "l2": "inputs larger than L2 (K alone is %.1f GB), no flush" % (nnz * 8 / 1e9)},
+            "iterations": it, "relres": infos[-1]["relres"], "rel_err": err64,
+            "rel_err_reference": "FP64 Jacobi-PCG on the GPU to relative residual 1e-13",
+            "breakdown_s": {"upload_pattern_assemble": float(np.mean([i["asm_s"] for i in infos])),
+                            "dirichlet_solve": float(np.mean([i["solve_s"] for i in infos]))},
+            "roofline": {"kernel": "k_spmv<double,3> (masked sliced-ELL 3x3-block SpMV, fused p.Ap)",
+                         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": spmv_bytes, "launch_ms": spmv_ms,
+                         "traffic": None},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+        })
+        if fp64_peak:
+            fl = 2.0 * nnz / (spmv_ms * 1e-3) / 1e12
+            line["fp64_pipe"] = {"spmv_tflops": fl, "probe_fp64_tflops": fp64_peak, "frac": fl / fp64_peak,
+                                 "probe_fp32_tflops": fp32_peak}
+    if "mixed" in args.legs:
         # ---- mixed precision on the same workload
         msm, infm, _ = timed(lambda: step(precision="mixed", precond="block_jacobi", profile=True),
                              args.steps, args.warmup)
         vmix, msm = aggregate(dist, n_dof, msm)
+        spmv32_ms = sum(i["ms_spmv"] for i in infm) / max(1, sum(i["spmv_launches"] for i in infm))
+        nnzb = nnz // 9
+        up_blocks = (nnzb - nN) // 2 + nN
+        lo_blocks = (nnzb - nN) // 2
+        sym_bytes = up_blocks * (36 + 4) + lo_blocks * 8 + 3 * nN * (4 + 4 + 1)
+        hbm_peak, peak_kind = measured_peaks()
         line["mixed"] = {"value": vmix, "ms_per_step": msm,
                          "precond": "block_jacobi", "iterations": infm[-1]["iterations"],
                          "fp64_refreshes": infm[-1]["reliable_updates"], "relres": infm[-1]["relres"],
-                         "rel_err": rel_err(dU), "speedup_vs_fp64": ms / msm,
-                         "spmv32_ms": sum(i["ms_spmv"] for i in infm) / max(1, sum(i["spmv_launches"] for i in infm))}
+                         "rel_err": rel_err(dU),
+                         "speedup_vs_fp64": (line["ms_per_step"] / msm) if "ms_per_step" in line else None,
+                         "spmv32": {"kernel": "k_spmv_sym<float,3> (upper-triangle 3x3 blocks, FP32)",
+                                    "launch_ms": spmv32_ms, "algorithmic_bytes_per_launch": sym_bytes,
+                                    "achieved_gbs": sym_bytes / (spmv32_ms * 1e-3) / 1e9,
+                                    "frac_hbm": sym_bytes / (spmv32_ms * 1e-3) / 1e9 / hbm_peak}}
+    if "e2e" in args.legs:
         # ---- e2e: C ABI with pinned host buffers, copies inside the timed region
         def pinned(a):
             t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
@@ -392,17 +410,17 @@ def our_arm(args, dist):
             K = pkg.assemble_system(p.ne, hX, hIEN, 3, "Q1", 3, hID, hY, 0.3, ctx=ctx, as_handle=True)
             K.solve(hFD, hFV, rtol=args.rtol, out=hU)
             K.close()
-        mse, _, _ = timed(step_e2e, args.steps, min(args.warmup, 1))
+        mse, _, _ = timed(step_e2e, args.steps, args.warmup)
         ve2e, mse = aggregate(dist, n_dof, mse)
         h2d = hX.nbytes + hIEN.nbytes + hID.nbytes + hY.nbytes + 8 + hFD.nbytes + hFV.nbytes
         line["e2e"] = {"value": ve2e, "unit": UNIT, "ms_per_step": mse,
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hU.nbytes),
                        "rel_err": float(np.linalg.norm(hU - uref_h) / np.linalg.norm(uref_h))}
+    if "cpu" in args.legs and dist.world == 1:
         # ---- CPU baseline (rank 0, N=1 only)
-        if dist.world == 1:
-            v, det = cpu_sample(pkg, args.ne, n_dof, nnz, it)
-            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",
-                                    "sample": det["sample"]}
+        v, det = cpu_sample(pkg, args.ne, n_dof, nnz, it)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",
+                                "sample": det["sample"]}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0

@@ -64,6 +64,7 @@ enum { SFEM_Q1 = 1, SFEM_Q2 = 2 };                      /* FunctionClass        
 enum { SFEM_PLANE_STRESS = 0, SFEM_PLANE_STRAIN = 1 };  /* 2D elasticity law          */
 enum { SFEM_FP64 = 0, SFEM_MIXED = 1 };                 /* solver precision           */
 enum { SFEM_PC_JACOBI = 0, SFEM_PC_BLOCK_JACOBI = 1 };  /* preconditioner             */
+enum { SFEM_FP32_UPPER = 0, SFEM_FP32_FULL = 1 };       /* mixed-precision K storage  */
 
 typedef struct sfem_ctx sfem_ctx;
 typedef struct sfem_mesh sfem_mesh;
@@ -190,6 +191,9 @@ typedef struct {
     double reliable_delta;/* mixed: refresh the FP64 residual when the FP32
                              residual has dropped by this factor                 */
     int profile;          /* 1: time the SpMV launches with CUDA events           */
+    int fp32_storage;     /* SFEM_MIXED: SFEM_FP32_UPPER (default) stores the
+                             upper-triangle blocks of K once (K is symmetric);
+                             SFEM_FP32_FULL keeps every block                    */
 } sfem_solve_opts;
 
 typedef struct {

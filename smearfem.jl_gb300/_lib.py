@@ -22,6 +22,7 @@ Q1, Q2 = 1, 2
 PLANE_STRESS, PLANE_STRAIN = 0, 1
 FP64, MIXED = 0, 1
 PC_JACOBI, PC_BLOCK_JACOBI = 0, 1
+FP32_UPPER, FP32_FULL = 0, 1
 
 
 class SfemError(RuntimeError):
@@ -35,7 +36,7 @@ class SfemError(RuntimeError):
 class SolveOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("precond", C.c_int), ("rtol", C.c_double),
                 ("maxit", C.c_int), ("check_every", C.c_int), ("reliable_delta", C.c_double),
-                ("profile", C.c_int)]
+                ("profile", C.c_int), ("fp32_storage", C.c_int)]
 
 
 class SolveStats(C.Structure):

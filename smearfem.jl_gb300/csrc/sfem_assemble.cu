@@ -382,6 +382,7 @@ extern "C" int sfem_matrix_destroy(sfem_matrix *K) {
         cudaSetDevice(ctx->device);
         sfem_dfree(ctx, K->val);
         sfem_dfree(ctx, K->val32);
+        sfem_sym_free(ctx, K);
         cudaStreamSynchronize(ctx->stream);
     }
     sfem_mesh_release(K->mesh);

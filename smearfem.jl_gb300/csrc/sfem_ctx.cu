@@ -237,6 +237,8 @@ extern "C" int sfem_ctx_create(int device, sfem_ctx **out) {
         sfem_ctx_destroy(c);
         return SFEM_CUDA_ERROR;
     }
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (c->num_sms < 1) c->num_sms = 1;
     // Keep freed pool memory for reuse by this process (large per-solve buffers).
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {

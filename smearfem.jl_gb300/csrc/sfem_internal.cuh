@@ -42,6 +42,7 @@ struct sfem_ctx {
     void *h_small = nullptr;    // pinned scratch for small read-backs (4 KB)
     std::string last_error;
     long long launches = 0;     // kernels launched through the library
+    int num_sms = 1;            // streaming multiprocessors of the device
 };
 
 struct sfem_mesh {
@@ -71,6 +72,13 @@ struct sfem_matrix {
     double *val = nullptr;     // FP64 blocks, SELL layout
     float *val32 = nullptr;    // FP32 copy (mixed precision), built on demand
     int64_t n = 0, nnz = 0;
+    // upper-triangle FP32 copy for the mixed solver (sfem_sym.cu), built on demand
+    int sym_state = 0;         // 0 not built, 1 ready, -1 not usable (full FP32 copy instead)
+    int64_t nslabsU = 0, nslabsL = 0;
+    int64_t *sptrU = nullptr, *sptrL = nullptr;
+    int *colU = nullptr;
+    int2 *lo = nullptr;
+    float *valU = nullptr;
 };
 
 // ---- host-side error helpers (sfem_ctx.cu) -------------------------------
@@ -119,3 +127,7 @@ int sfem_element_stiffness(sfem_ctx *ctx, const sfem_mesh *m, int plane, const d
                            int64_t nYoung, const double *dnu, int64_t nNu, double *kbuf);
 int sfem_gather_blocks(sfem_ctx *ctx, const sfem_mesh *m, const double *kbuf, double *val,
                        float *val32);
+// Upper-triangle FP32 copy of K (sfem_sym.cu).
+int sfem_sym_build(sfem_ctx *ctx, sfem_matrix *K);
+int sfem_sym_refresh_values(sfem_ctx *ctx, sfem_matrix *K);
+void sfem_sym_free(sfem_ctx *ctx, sfem_matrix *K);

@@ -107,5 +107,6 @@ extern "C" int sfem_reassemble_noalloc(sfem_ctx *ctx, sfem_matrix *K, const doub
             SFEM_LAUNCHED(ctx);
         }
     }
+    SFEM_TRY(sfem_sym_refresh_values(ctx, K));  // and its upper-triangle FP32 copy (no allocation)
     return sfem_check_device(ctx, "no-alloc re-assembly");
 }

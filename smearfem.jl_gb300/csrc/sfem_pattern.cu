@@ -78,23 +78,28 @@ __global__ void k_n2e_sort(const int64_t *__restrict__ ptr, int *__restrict__ n2
 }
 
 // Referenced nodes: validate their ID entries and find the matrix size.
+// *maxg receives (largest referenced DOF index) + 1; a warp-level max goes
+// first so the single-address atomic sees one request per warp.
 __global__ void k_dof_extent(const int64_t *__restrict__ ptr, const int *__restrict__ id, int64_t nN,
-                             int b, unsigned long long *__restrict__ maxg, DevErr *err) {
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nN) return;
-    if (ptr[r + 1] == ptr[r]) return;  // not used by any element
-    if (b == 1) {
-        atomicMax(maxg, (unsigned long long)r);
-        return;
-    }
-    for (int d = 0; d < b; ++d) {
-        int g = id[(int64_t)d * nN + r];
-        if (g < 0) {
-            sfem_dev_error(err, SFEM_BAD_INDEX, r);
-            continue;
+                             int b, unsigned int *__restrict__ maxg, DevErr *err) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned int v = 0;
+    if (r < nN && ptr[r + 1] != ptr[r]) {  // nodes no element uses do not count
+        if (b == 1) {
+            v = (unsigned int)r + 1u;
+        } else {
+            for (int d = 0; d < b; ++d) {
+                const int g = id[(int64_t)d * nN + r];
+                if (g < 0) {
+                    sfem_dev_error(err, SFEM_BAD_INDEX, r);
+                    continue;
+                }
+                v = max(v, (unsigned int)g + 1u);
+            }
         }
-        atomicMax(maxg, (unsigned long long)g);
     }
+    v = __reduce_max_sync(0xffffffffu, v);  // blocks are whole warps; no thread has returned
+    if ((threadIdx.x & 31) == 0 && v) atomicMax(maxg, v);
 }
 
 __global__ void k_g2i(const int64_t *__restrict__ ptr, const int *__restrict__ id, int64_t nN, int b,
@@ -380,15 +385,17 @@ extern "C" int sfem_pattern_build(sfem_ctx *ctx, sfem_mesh *m, int64_t *n_out, i
         SFEM_LAUNCHED(ctx);
 
         // matrix size and global DOF -> internal index
-        unsigned long long *dmax = (unsigned long long *)cursor;  // reuse
-        if ((st = sfem_cuda_status(ctx, cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s), "memset")))
+        unsigned int *dmax = (unsigned int *)cursor;  // reuse
+        if ((st = sfem_cuda_status(ctx, cudaMemsetAsync(dmax, 0, sizeof(unsigned int), s), "memset")))
             break;
         k_dof_extent<<<blocks_for(nN, 256), 256, 0, s>>>(m->n2e_ptr, m->id, nN, b, dmax, ctx->d_err);
         SFEM_LAUNCHED(ctx);
         unsigned long long *h = (unsigned long long *)ctx->h_small;
-        if ((st = sfem_cuda_status(ctx, cudaMemcpyAsync(h, dmax, 8, cudaMemcpyDeviceToHost, s), "memcpy"))) break;
+        unsigned int *h32 = (unsigned int *)ctx->h_small;
+        if ((st = sfem_cuda_status(ctx, cudaMemcpyAsync(h32, dmax, 4, cudaMemcpyDeviceToHost, s), "memcpy")))
+            break;
         if ((st = sfem_check_device(ctx, "ID validation"))) break;
-        int64_t ng = nEl > 0 ? (int64_t)h[0] + 1 : 0;
+        int64_t ng = (int64_t)h32[0];
         m->n_global = ng;
         if ((st = sfem_dalloc(ctx, (void **)&m->g2i, sizeof(int) * (ng ? ng : 1), "g2i"))) break;
         if ((st = sfem_cuda_status(ctx, cudaMemsetAsync(m->g2i, 0xff, sizeof(int) * (ng ? ng : 1), s), "memset")))

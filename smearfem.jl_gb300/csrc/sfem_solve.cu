@@ -40,6 +40,7 @@ namespace {
 
 constexpr int SPMV_T = 256;
 constexpr int UPD_T = 256;
+constexpr int UPD_NODES = 128;  // nodes per CTA of k_update (B * 128 threads)
 
 struct CgScalars {
     double rz, rz_prev, pAp, alpha, beta, rr, bb, tol2, rr_ref, delta2;
@@ -121,9 +122,10 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
     if (MODE == 1 && S->done) return;
     if (MODE == 2 && !S->refresh) return;
     const int lane = threadIdx.x & 31;
-    const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     double dot = 0.0;
-    if (s < nslices) {
+    // one warp per 32-row slice; grid-stride so a small grid can cover all slices
+    for (int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nwarps) {
         const int64_t r = s * 32 + lane;
         const int64_t slab0 = sliceptr[s], slab1 = sliceptr[s + 1];
         T acc[B];
@@ -172,41 +174,131 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
     }
 }
 
+// The same product from the upper-triangle copy (sfem_sym.cu):
+// y_r = sum_{c>=r} A_rc x_c + sum_{c<r} A_cr^T x_c, one lane per row.
+template <typename T, int B, int MODE>
+__global__ void __launch_bounds__(SPMV_T)
+k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, const T *__restrict__ valU,
+           const int64_t *__restrict__ sptrL, const int2 *__restrict__ lo, int64_t nN, int64_t nslices,
+           const T *__restrict__ x, T *__restrict__ y, const unsigned char *__restrict__ fixed, CgScalars *S,
+           double *partial) {
+    if (MODE == 1 && S->done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    double dot = 0.0;
+    for (int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nwarps) {
+        const int64_t r = s * 32 + lane;
+        T acc[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) acc[i] = T(0);
+        // upper and lower parts in one loop: the lower part's loads depend on
+        // its index entry, the upper part's do not, so interleaving them keeps
+        // more independent loads in flight; the next index entry is prefetched.
+        const int64_t u0 = sptrU[s], nu = sptrU[s + 1] - u0;
+        const int64_t l0 = sptrL[s], nl = sptrL[s + 1] - l0;
+        const int64_t nk = nu > nl ? nu : nl;
+        int2 ent_next = nl > 0 ? __ldg(&lo[l0 * 32 + lane]) : make_int2(-1, 0);
+        for (int64_t k = 0; k < nk; ++k) {
+            const int2 ent = ent_next;
+            if (k + 1 < nl) ent_next = __ldg(&lo[(l0 + k + 1) * 32 + lane]);
+            if (k < nu) {
+                const int64_t su = u0 + k;
+                const int c = __ldg(&colU[su * 32 + lane]);
+                T v[B * B];
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) v[e] = __ldg(&valU[(su * B * B + e) * 32 + lane]);
+                T xc[B];
+#pragma unroll
+                for (int j = 0; j < B; ++j) xc[j] = __ldg(&x[(int64_t)c * B + j]);
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) acc[i] = fma(v[i * B + j], xc[j], acc[i]);
+            }
+            if (k < nl && ent.x >= 0) {  // ent.x < 0: padding
+                const int c = ent.y;
+                T v[B * B];
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) v[e] = __ldg(&valU[ent.x + e * 32]);
+                T xc[B];
+#pragma unroll
+                for (int j = 0; j < B; ++j) xc[j] = __ldg(&x[(int64_t)c * B + j]);
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) acc[i] = fma(v[j * B + i], xc[j], acc[i]);
+            }
+        }
+        if (r < nN) {
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                const int64_t d = r * B + i;
+                const T out = fixed[d] ? T(0) : acc[i];
+                y[d] = out;
+                if (MODE == 1) dot += (double)(x[d] * out);
+            }
+        }
+    }
+    if (MODE == 1) {
+        double tot, dummy;
+        if (reduce2_last(dot, 0.0, partial, &S->ticket[0], &tot, &dummy) && threadIdx.x == 0) {
+            S->pAp = tot;
+            if (!(tot > 0.0)) {
+                S->status = SFEM_SINGULAR;
+                S->done = 1;
+                S->alpha = 0.0;
+            } else {
+                S->alpha = S->rz / tot;
+            }
+        }
+    }
+}
+
 // x += alpha p; r -= alpha q; z = M^-1 r; reduce r.z and r.r; CG scalar update.
 // PC: 0 Jacobi (minv per DOF), 1 block-Jacobi (minv: B x B per node).
 // MIXED: the recursive FP32 residual never ends the solve; reaching the
 // tolerance, dropping by delta since the last refresh, or hitting maxit
 // requests an FP64 refresh instead (k_fold / k_spmv MODE 2 / k_refresh).
 template <typename T, int B, int PC, bool MIXED>
-__global__ void __launch_bounds__(UPD_T)
+__global__ void __launch_bounds__(UPD_NODES * B)
 k_update(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
          const T *__restrict__ q, const T *__restrict__ minv, CgScalars *S, double *partial) {
     if (S->done) return;
-    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // one thread per DOF (coalesced vector traffic); a CTA walks tiles of
+    // UPD_NODES whole nodes, whose residuals are staged in shared memory for
+    // the nodal block-Jacobi product.  The grid is sized to what is resident,
+    // so each launch pays few per-CTA reductions.
+    __shared__ T rs[UPD_NODES * B];
+    const int64_t nd = nN * B;
+    const T alpha = (T)S->alpha;
     double rz = 0.0, rr = 0.0;
-    if (node < nN) {
-        const T alpha = (T)S->alpha;
-        T rv[B];
-#pragma unroll
-        for (int i = 0; i < B; ++i) {
-            const int64_t d = node * B + i;
+    const int64_t ntiles = sfem_cdiv(nN, UPD_NODES);
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {  // uniform trip count per CTA
+        const int64_t d = tile * (UPD_NODES * B) + threadIdx.x;
+        T rv = T(0);
+        if (d < nd) {
             x[d] = fma(alpha, p[d], x[d]);
-            rv[i] = fma(-alpha, q[d], r[d]);
-            r[d] = rv[i];
+            rv = fma(-alpha, q[d], r[d]);
+            r[d] = rv;
         }
+        T zi = T(0);
+        if (PC == 0 || B == 1) {
+            if (d < nd) zi = minv[d] * rv;
+        } else {
+            __syncthreads();  // rs of the previous tile is no longer read
+            rs[threadIdx.x] = rv;
+            __syncthreads();
+            if (d < nd) {
+                const int nl = threadIdx.x / B;
+                const T *mrow = minv + d * B;  // row (node*B + i) of the node's block
 #pragma unroll
-        for (int i = 0; i < B; ++i) {
-            T zi;
-            if (PC == 0) {
-                zi = minv[node * B + i] * rv[i];
-            } else {
-                zi = T(0);
-#pragma unroll
-                for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], rv[j], zi);
+                for (int j = 0; j < B; ++j) zi = fma(mrow[j], rs[nl * B + j], zi);
             }
-            z[node * B + i] = zi;
-            rz += (double)(rv[i] * zi);
-            rr += (double)(rv[i] * rv[i]);
+        }
+        if (d < nd) {
+            z[d] = zi;
+            rz += (double)(rv * zi);
+            rr += (double)(rv * rv);
         }
     }
     double trz, trr;
@@ -389,10 +481,10 @@ __global__ void k_cast(int64_t n, const double *__restrict__ a, T *__restrict__ 
 
 __global__ void k_fold(int64_t n, double *__restrict__ x64, float *__restrict__ x32, const CgScalars *S) {
     if (!S->refresh) return;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    x64[i] += (double)x32[i];
-    x32[i] = 0.0f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x64[i] += (double)x32[i];
+        x32[i] = 0.0f;
+    }
 }
 
 // r64 = b - Kx64 (masked), r32 = (float) r64, z32 = M^-1 r32; reduce r.z, r.r.
@@ -402,9 +494,9 @@ k_refresh(int64_t nN, const double *__restrict__ bvec, const double *__restrict_
           double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ z32, const float *__restrict__ minv,
           CgScalars *S, double *partial) {
     if (!S->refresh) return;
-    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double rz = 0.0, rr = 0.0;
-    if (node < nN) {
+    for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < nN;
+         node += (int64_t)gridDim.x * blockDim.x) {
         float rv[B];
 #pragma unroll
         for (int i = 0; i < B; ++i) {
@@ -505,6 +597,18 @@ struct Vecs {
     T *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *minv = nullptr;
 };
 
+// Grid that fills the GPU once: resident CTAs per SM x SMs, capped at `need`.
+template <typename K>
+unsigned resident_grid(sfem_ctx *ctx, K kernel, int threads, int64_t need) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const int64_t g = (int64_t)per_sm * ctx->num_sms;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, need > 0 ? need : 1));
+}
+
 class Solver {
    public:
     Solver(sfem_ctx *c, sfem_matrix *K, const sfem_solve_opts &o) : ctx(c), K(K), m(K->mesh), opts(o) {}
@@ -542,7 +646,7 @@ class Solver {
     double *ud = nullptr, *bvec = nullptr, *partial = nullptr;
     CgScalars *S = nullptr;
     int64_t nd = 0;  // internal DOFs = nN * b
-    unsigned spmv_grid = 1, upd_grid = 1, vec_grid = 1;
+    unsigned spmv_grid = 1, upd_grid = 1, vec_grid = 1, upd2_grid = 1;
     cudaGraphExec_t gexec = nullptr;
     std::vector<cudaEvent_t> events;
     double ms_spmv = 0.0;
@@ -555,12 +659,30 @@ class Solver {
 
 template <typename T, int B>
 void Solver::launch_spmv(const T *val, const T *x, T *y, bool fused) {
-    if (fused)
-        k_spmv<T, B, 1><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(m->sliceptr, m->col, val, m->nN, m->nslices, x, y,
-                                                               fixed, S, partial);
-    else
-        k_spmv<T, B, 0><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(m->sliceptr, m->col, val, m->nN, m->nslices, x, y,
-                                                               fixed, S, partial);
+    if constexpr (sizeof(T) == 4) {
+        if (K->sym_state == 1 && opts.fp32_storage == SFEM_FP32_UPPER) {
+            if (fused) {
+                auto kern = k_spmv_sym<float, B, 1>;
+                kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+                    K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial);
+            } else {
+                auto kern = k_spmv_sym<float, B, 0>;
+                kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+                    K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial);
+            }
+            SFEM_LAUNCHED(ctx);
+            return;
+        }
+    }
+    if (fused) {
+        auto kern = k_spmv<T, B, 1>;
+        kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+            m->sliceptr, m->col, val, m->nN, m->nslices, x, y, fixed, S, partial);
+    } else {
+        auto kern = k_spmv<T, B, 0>;
+        kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+            m->sliceptr, m->col, val, m->nN, m->nslices, x, y, fixed, S, partial);
+    }
     SFEM_LAUNCHED(ctx);
 }
 
@@ -584,16 +706,21 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
         if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
         launch_spmv<T, B>(val, v.p, v.q, true);
         if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
-        k_update<T, B, PC, MIXED><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.x, v.r, v.z, v.p, v.q, v.minv, S,
-                                                                       partial);
+        {
+            auto kern = k_update<T, B, PC, MIXED>;
+            kern<<<resident_grid(ctx, kern, UPD_NODES * B, upd2_grid), UPD_NODES * B, 0, ctx->stream>>>(
+                m->nN, v.x, v.r, v.z, v.p, v.q, v.minv, S, partial);
+        }
         SFEM_LAUNCHED(ctx);
         if constexpr (MIXED) {
             // FP64 refresh, skipped on the device unless k_update requested it
-            k_fold<<<vec_grid, 256, 0, ctx->stream>>>(nd, x64, (float *)v.x, S);
-            k_spmv<double, B, 2><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(m->sliceptr, m->col, K->val, m->nN,
-                                                                       m->nslices, x64, q64, fixed, S, partial);
-            k_refresh<B, PC><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, bvec, q64, fixed, r64, (float *)v.r,
-                                                                  (float *)v.z, (const float *)v.minv, S, partial);
+            // small grid-stride grids: these launches exit at once on most iterations
+            const unsigned small = (unsigned)(4 * ctx->num_sms);
+            k_fold<<<std::min(vec_grid, small), 256, 0, ctx->stream>>>(nd, x64, (float *)v.x, S);
+            k_spmv<double, B, 2><<<std::min(spmv_grid, small), SPMV_T, 0, ctx->stream>>>(
+                m->sliceptr, m->col, K->val, m->nN, m->nslices, x64, q64, fixed, S, partial);
+            k_refresh<B, PC><<<std::min(upd_grid, small), UPD_T, 0, ctx->stream>>>(
+                m->nN, bvec, q64, fixed, r64, (float *)v.r, (float *)v.z, (const float *)v.minv, S, partial);
             ctx->launches += 3;
         }
     };
@@ -685,7 +812,8 @@ int Solver::solve_b(double *x64) {
         SFEM_TRY(block ? cg_loop<double, B, 1, false>(v, nullptr, nullptr, nullptr)
                        : cg_loop<double, B, 0, false>(v, nullptr, nullptr, nullptr));
     } else {
-        if (!K->val32) {
+        if (opts.fp32_storage == SFEM_FP32_UPPER && K->sym_state == 0) SFEM_TRY(sfem_sym_build(ctx, K));
+        if ((K->sym_state != 1 || opts.fp32_storage == SFEM_FP32_FULL) && !K->val32) {
             const int64_t nv = m->nslabs * 32 * B * B;
             SFEM_TRY(sfem_dalloc(ctx, (void **)&K->val32, sizeof(float) * (nv ? nv : 1), "FP32 K values"));
             k_cast<float><<<(unsigned)sfem_cdiv(nv > 0 ? nv : 1, 256), 256, 0, ctx->stream>>>(nv, K->val, K->val32);
@@ -725,6 +853,7 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
     nd = m->nN * b;
     spmv_grid = (unsigned)sfem_cdiv(m->nslices * 32 > 0 ? m->nslices * 32 : 1, SPMV_T);
     upd_grid = (unsigned)sfem_cdiv(m->nN, UPD_T);
+    upd2_grid = (unsigned)sfem_cdiv(m->nN > 0 ? m->nN : 1, UPD_NODES);
     vec_grid = (unsigned)sfem_cdiv(nd, 256);
     const long long launches0 = ctx->launches;
 
@@ -737,7 +866,8 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
     SFEM_TRY(alloc(&x64, nd, "x"));
     SFEM_TRY(alloc(&ug, n, "u"));
     SFEM_TRY(alloc(&S, 1, "CG scalars"));
-    SFEM_TRY(alloc(&partial, 2 * (int64_t)std::max(spmv_grid, std::max(upd_grid, vec_grid)), "partials"));
+    SFEM_TRY(alloc(&partial, 2 * (int64_t)std::max(std::max(spmv_grid, upd2_grid), std::max(upd_grid, vec_grid)),
+                   "partials"));
     SFEM_TRY(alloc(&dfix, nfix, "fixed dofs"));
     SFEM_TRY(alloc(&dvals, nfix, "fixed values"));
     SFEM_TRY(sfem_copy_in(ctx, dfix, fixed_dofs, sizeof(int64_t) * nfix, mem_space));
@@ -859,6 +989,7 @@ extern "C" void sfem_solve_opts_default(sfem_solve_opts *o) {
     o->check_every = 32;
     o->reliable_delta = 0.1;
     o->profile = 0;
+    o->fp32_storage = SFEM_FP32_UPPER;
 }
 
 extern "C" int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t *fixed_dofs, int64_t nfix,
@@ -872,6 +1003,7 @@ extern "C" int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t
     if (opts) o = *opts;
     if (!(o.rtol >= 0.0) || o.maxit < 0 || (o.precision != SFEM_FP64 && o.precision != SFEM_MIXED) ||
         (o.precond != SFEM_PC_JACOBI && o.precond != SFEM_PC_BLOCK_JACOBI) || !(o.reliable_delta > 0.0) ||
+        (o.fp32_storage != SFEM_FP32_UPPER && o.fp32_storage != SFEM_FP32_FULL) ||
         !(o.reliable_delta < 1.0))
         return sfem_set_error(ctx, SFEM_BAD_ARG, "bad solve options");
     if (stats) memset(stats, 0, sizeof(*stats));

@@ -265,7 +265,7 @@ class Matrix:
 
     def solve(self, fixed_dofs, fixed_vals, f=None, precision="fp64", precond="jacobi",
               rtol=1e-10, maxit=100000, check_every=32, reliable_delta=0.1, profile=False,
-              out=None):
+              out=None, fp32_storage="upper"):
         """Dirichlet solve (examples/vector3D.jl:314-322); returns ``(u, stats)``.
 
         ``fixed_dofs`` are 1-based global DOF ids.  ``out`` may be a device
@@ -280,6 +280,7 @@ class Matrix:
         opts.check_every = check_every
         opts.reliable_delta = reliable_delta
         opts.profile = 1 if profile else 0
+        opts.fp32_storage = {"upper": L.FP32_UPPER, "full": L.FP32_FULL}[fp32_storage]
         Fd = _Buf(fixed_dofs, np.int64)
         Fv = _Buf(fixed_vals, np.float64)
         Ff = _Buf(f, np.float64)

@@ -31,6 +31,7 @@ struct SolveOpts
     check_every::Cint
     reliable_delta::Cdouble
     profile::Cint
+    fp32_storage::Cint
 end
 
 mutable struct SolveStats
@@ -163,7 +164,7 @@ function solve_dirichlet(K::GPUMatrix, fixed_dofs, fixed_vals, f=nothing; precis
     fd = Int64.(collect(fixed_dofs)); fv = Float64.(collect(fixed_vals))
     fp = f === nothing ? C_NULL : Float64.(collect(f))
     u = Vector{Float64}(undef, K.n)
-    opts = SolveOpts(precision == :mixed ? 1 : 0, precond == :block_jacobi ? 1 : 0, rtol, maxit, 32, 0.1, 0)
+    opts = SolveOpts(precision == :mixed ? 1 : 0, precond == :block_jacobi ? 1 : 0, rtol, maxit, 32, 0.1, 0, 0)
     stats = SolveStats()
     GC.@preserve fd fv fp u begin
         st = ccall((:sfem_solve_dirichlet, libsfem), Cint,

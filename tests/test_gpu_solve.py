@@ -133,3 +133,40 @@ def test_repeatable_bitwise(sfem, ctx):
         a, _ = K.solve(p.fixed_dofs, p.fixed_vals, precision=precision)
         b, _ = K.solve(p.fixed_dofs, p.fixed_vals, precision=precision)
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("storage", ["upper", "full"])
+@pytest.mark.parametrize("precond", ["jacobi", "block_jacobi"])
+def test_mixed_fp32_storages(sfem, ctx, storage, precond):
+    """The mixed solver's FP32 K as upper-triangle blocks (default) or full
+    blocks: both reach the FP64 solution within 1e-8."""
+    p = sfem.meshgen.config3(ne=12)
+    K = _handle(sfem, ctx, p)
+    ref, _ = K.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13)
+    u, st = K.solve(p.fixed_dofs, p.fixed_vals, precision="mixed", precond=precond, rtol=1e-11,
+                    fp32_storage=storage)
+    assert st["status"] == 0 and st["reliable_updates"] >= 1
+    assert _rel(u, ref) <= TOL_U
+
+
+def test_mixed_upper_storage_general_id(sfem, ctx, oracle):
+    """Upper-triangle FP32 storage on a permuted ID with unused nodes."""
+    ne = 5
+    NL, IEN, ID, _, _ = sfem.meshgen.meshgrid(0, 1, 0, 1, 0, 1, ne, 3)
+    rng = np.random.default_rng(12)
+    NL = sfem.meshgen.jitter_interior(NL, ne, 0.2, rng)
+    nN = NL.shape[1]
+    NL = np.concatenate([NL, rng.uniform(0, 1, (3, 3))], axis=1)
+    ID2 = (rng.permutation(3 * (nN + 3)) + 1).reshape(nN + 3, 3)
+    bot = np.flatnonzero(NL[2, :nN] == 0)
+    top = np.flatnonzero(NL[2, :nN] == 1)
+    fixed = np.concatenate([ID2[bot].ravel(), ID2[top, 2], ID2[nN:].ravel()])
+    vals = np.concatenate([np.zeros(3 * bot.size), 0.01 * np.sin(np.pi * NL[0, top]),
+                           np.zeros(9)])
+    Kref = oracle.assemble_system(ne, NL, IEN, 3, "Q1", 3, ID2, 1.0, 0.3)
+    n = Kref[4]
+    keep = fixed <= n
+    uref = oracle.solve_eliminated(Kref, fixed[keep], vals[keep], method="inv")
+    K = sfem.assemble_system(ne, NL, IEN, 3, "Q1", 3, ID2, 1.0, 0.3, ctx=ctx, as_handle=True)
+    u, st = K.solve(fixed[keep], vals[keep], precision="mixed", precond="block_jacobi", rtol=1e-12)
+    assert _rel(u, uref) <= TOL_U
