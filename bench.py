@@ -55,8 +55,9 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ne", type=int, default=128)
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--legs", default="value,mixed,e2e,cpu",
-                    help="comma list of value,mixed,e2e,cpu (profiling runs pick one)")
+    ap.add_argument("--legs", default="value,mixed,e2e,cpu,batch",
+                    help="comma list of value,mixed,e2e,cpu,batch (profiling runs pick one)")
+    ap.add_argument("--batch-count", type=int, default=1024, help="meshes in the batch leg")
     ap.add_argument("--no-extras", action="store_true", help="same as --legs value")
     a = ap.parse_args(argv)
     a.legs = {"value"} if a.no_extras else set(x.strip() for x in a.legs.split(",") if x.strip())
@@ -416,6 +417,8 @@ def our_arm(args, dist):
         line["e2e"] = {"value": ve2e, "unit": UNIT, "ms_per_step": mse,
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hU.nbytes),
                        "rel_err": float(np.linalg.norm(hU - uref_h) / np.linalg.norm(uref_h))}
+    if "batch" in args.legs:
+        line["batch"] = batch_leg(args, pkg, ctx, stream, dist)
     if "cpu" in args.legs and dist.world == 1:
         # ---- CPU baseline (rank 0, N=1 only)
         v, det = cpu_sample(pkg, args.ne, n_dof, nnz, it)
@@ -424,6 +427,71 @@ def our_arm(args, dist):
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def batch_leg(args, pkg, ctx, stream, dist):
+    """Batching workload: ``batch_count`` plane-strain unit squares, n ~ U{16..256},
+    jitter 0.15h, E = 1, nu_mesh ~ U(0.2, 0.45), clamped left edge, 3-mode right
+    edge u_x; mixed-precision block-Jacobi PCG to 1e-8 in one persistent launch.
+    Beside it: the plain FP64 GPU path (single-mesh API, Jacobi-PCG, one mesh
+    after another) on the same meshes."""
+    import torch
+    probs = pkg.meshgen.config4(count=args.batch_count)
+    n_total = int(sum(p.n_dof for p in probs))
+    nus = np.array([float(p.nu[0]) for p in probs])
+    fixed = [p.fixed_dofs for p in probs]
+    vals = [p.fixed_vals for p in probs]
+    t0 = time.perf_counter()
+    bt = pkg.Batch.from_problems(probs, ctx=ctx)
+    t_setup = time.perf_counter() - t0
+    rtol = 1e-8
+
+    def run_batch():
+        return bt.solve(1.0, nus, fixed, vals, plane="strain", precision="mixed",
+                        precond="block_jacobi", rtol=rtol)
+
+    for _ in range(args.warmup):
+        u, st = run_batch()
+    dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        u, st = run_batch()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    value, ms = aggregate(dist, n_total, ms)
+    parts = bt.split(u)
+    # plain FP64 GPU path, one mesh after another, same stopping rule
+    t0 = time.perf_counter()
+    plain_u = []
+    for p in probs:
+        K = pkg.assemble_system(p.ne, p.NodeList, p.IEN, 2, "Q1", 2, p.ID, 1.0, float(p.nu[0]),
+                                plane="strain", ctx=ctx, as_handle=True)
+        plain_u.append(K.solve(p.fixed_dofs, p.fixed_vals, rtol=rtol)[0])
+        K.close()
+    t_plain = time.perf_counter() - t0
+    # error against tight FP64 solves on a sample of meshes
+    errs = []
+    for k in range(0, len(probs), max(1, len(probs) // 32)):
+        p = probs[k]
+        K = pkg.assemble_system(p.ne, p.NodeList, p.IEN, 2, "Q1", 2, p.ID, 1.0, float(p.nu[0]),
+                                plane="strain", ctx=ctx, as_handle=True)
+        ref = K.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13)[0]
+        K.close()
+        errs.append(float(np.linalg.norm(parts[k] - ref) / np.linalg.norm(ref)))
+    bt.close()
+    its = np.array([s["iterations"] for s in st])
+    return {"workload": f"{len(probs)} plane-strain Q1 quad meshes, n ~ U{{16..256}}, mixed "
+                        f"block-Jacobi PCG to {rtol:g}, one persistent launch",
+            "n_dof_total": n_total, "value": value, "unit": UNIT, "ms_per_batch": ms,
+            "setup_s": t_setup, "statuses_ok": int(sum(s["status"] == 0 for s in st)),
+            "iterations": {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())},
+            "rel_err_max_sample": max(errs), "rel_err_reference": "FP64 PCG to 1e-13 on every "
+            f"{max(1, len(probs) // 32)}th mesh",
+            "plain_fp64_gpu": {"value": n_total / t_plain, "s": t_plain,
+                               "path": "single-mesh API per mesh: assemble + FP64 Jacobi-PCG"},
+            "speedup_vs_plain_fp64": (n_total / (ms * 1e-3)) / (n_total / t_plain)}
 
 
 def main(argv=None):

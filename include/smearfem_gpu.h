@@ -220,6 +220,61 @@ SFEM_API int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t *
                          double *u_out, int mem_space, const sfem_solve_opts *opts,
                          sfem_solve_stats *stats);
 
+/* ---- batches of independent meshes ---------------------------------------- */
+
+/* Many independent meshes of one element class, assembled and solved together
+ * by one persistent kernel (no reference counterpart: the reference solves one
+ * mesh per call, examples/vector3D.jl:305-322).  Each mesh gets its own
+ * Jacobian/assembly, Dirichlet elimination and CG; results do not depend on
+ * what else is in the batch. */
+typedef struct sfem_batch sfem_batch;
+
+typedef struct {
+    int status;      /* sfem_status of this mesh's solve                    */
+    int iterations;  /* CG iterations                                       */
+    int refreshes;   /* FP64 residual refreshes (SFEM_MIXED)                */
+    int reserved;
+    double relres;   /* relative residual at exit (FP64 true residual for
+                        SFEM_MIXED, recursive residual for SFEM_FP64)        */
+} sfem_batch_stats;
+
+/* Upload nmesh meshes.  Mesh m owns nodes [node_offsets[m], node_offsets[m+1])
+ * of NodeList (ndim x total nodes) and elements [elem_offsets[m],
+ * elem_offsets[m+1]) of IEN (total elements x nen, column-major); IEN and ID
+ * entries are 1-based and local to their mesh.  ID (total nodes x nDof,
+ * column-major) may be NULL for the interleaved numbering ID[k,l] =
+ * nDof*(k-1)+l (examples/vector3D.jl:73-75); its entries must lie in
+ * 1..nDof*(mesh nodes).  Builds the sparsity pattern of every mesh. */
+SFEM_API int sfem_batch_create(sfem_ctx *ctx, int ndim, int function_class, int nDof, int64_t nmesh,
+                               const int64_t *node_offsets, const int64_t *elem_offsets,
+                               const double *NodeList, const int64_t *IEN, const int64_t *ID,
+                               int mem_space, sfem_batch **out);
+
+/* total_dofs = nDof * total nodes: the length of u in sfem_batch_solve. */
+SFEM_API int sfem_batch_info(const sfem_batch *batch, int64_t *total_dofs, int64_t *total_nodes,
+                             int64_t *total_elements);
+
+/* Launch shape of the persistent kernel: threads per CTA (256 or 512) and
+ * CTAs per SM (capped by occupancy).  sfem_batch_autotune picks them. */
+SFEM_API int sfem_batch_set_launch(sfem_batch *batch, int threads, int ctas_per_sm);
+
+/* Assemble and solve every mesh in one persistent kernel launch.
+ *   Young/nu: length 1 (all), nmesh (per mesh) or total elements.
+ *   fix_offsets (nmesh+1): mesh m's prescribed DOFs are entries
+ *   [fix_offsets[m], fix_offsets[m+1]) of fixed_dofs (1-based, local to the
+ *   mesh) and fixed_vals.
+ *   u_out (total_dofs): mesh m's displacement starts at nDof*node_offsets[m],
+ *   in its ID numbering.
+ *   opts: precision, precond, rtol, maxit, reliable_delta are used.
+ *   stats: nmesh entries (may be NULL).  The call returns SFEM_OK when the
+ *   launch ran; per-mesh outcomes are in stats. */
+SFEM_API int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *batch, int plane, const double *Young,
+                              int64_t nYoung, const double *nu, int64_t nNu,
+                              const int64_t *fix_offsets, const int64_t *fixed_dofs,
+                              const double *fixed_vals, double *u_out, int mem_space,
+                              const sfem_solve_opts *opts, sfem_batch_stats *stats);
+SFEM_API int sfem_batch_destroy(sfem_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,1072 @@
+// Batches of independent meshes, assembled and solved by ONE persistent kernel.
+//
+// Layout.  The meshes of a batch become one block-diagonal "combined" mesh:
+// mesh b's nodes are renumbered into [pad_base[b], pad_base[b] + nN_b) with
+// every range padded to a multiple of 32, so each 32-row slice of the
+// sliced-ELL pattern belongs to exactly one mesh.  The pattern of the
+// combined mesh is built once (sfem_batch_create) with the single-mesh
+// kernels; its rows never couple two meshes.
+//
+// Solve.  k_batch runs with a grid sized to fill the GPU once.  Each CTA
+// takes meshes from an atomic work queue, largest first, and for each one:
+//   1. element stiffness of the mesh's elements (FP64, as k_element),
+//   2. deterministic gather into the mesh's K blocks (as k_gather), FP64 and
+//      an FP32 copy for the mixed solver,
+//   3. Dirichlet set-up: mask, lift q_d, right-hand side -K q_d,
+//   4. nodal block-Jacobi inverse,
+//   5. preconditioned CG: FP64, or FP32 recurrences refreshed from an FP64
+//      residual whenever the FP32 residual drops by `reliable_delta`,
+//   6. u = q_d + x in the mesh's own DOF numbering.
+// All reductions are CTA-wide in a fixed order and no CTA ever waits on
+// another, so a mesh's result does not depend on which CTA solves it or on
+// what else is in the batch: it is bitwise the same alone and in any mix.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <type_traits>
+#include <vector>
+
+#include "sfem_internal.cuh"
+
+struct BatchMesh {
+    int64_t node0, nnode;      // combined (padded) node range start, real node count
+    int64_t slice0, slice1;    // its slices
+    int64_t elem0, elem1;      // its elements in the combined numbering
+    int64_t dof0, ndof;        // its block of u: global DOFs [dof0, dof0 + ndof)
+    int64_t fix0, fix1;        // its entries of the fixed-DOF arrays
+};
+
+struct sfem_batch {
+    sfem_ctx *ctx = nullptr;
+    sfem_mesh *mesh = nullptr;  // combined mesh (owns the pattern)
+    int ndim = 0, nen = 0, b = 1, fclass = 1;
+    int64_t nmesh = 0, total_nodes = 0, total_elems = 0, total_dofs = 0;
+    std::vector<int64_t> h_node_off, h_elem_off, h_pad_base;
+    BatchMesh *meshes = nullptr;  // device
+    int *order = nullptr;         // device: meshes by decreasing size
+    unsigned *queue = nullptr;    // device work counter
+    // solve buffers (allocated at the first solve, reused)
+    bool buffers = false;
+    double *kbuf = nullptr, *val64 = nullptr, *ud = nullptr, *b64 = nullptr, *x64 = nullptr, *q64 = nullptr;
+    float *val32 = nullptr;
+    void *vecT = nullptr;         // 5 work vectors of the CG type + preconditioner
+    unsigned char *fixed = nullptr, *gfixed = nullptr;
+    double *E = nullptr, *nu = nullptr, *fvals = nullptr, *u = nullptr;
+    int64_t *fdofs = nullptr, *fix_off_dev = nullptr;
+    int64_t cap_E = 0, cap_nu = 0, cap_fixd = 0, cap_fixv = 0;
+    int threads = 512, ctas_per_sm = 1;  // launch shape (autotuned)
+};
+
+namespace {
+
+struct ElemTableB {
+    double dN[8][9][3];
+    double w[8];
+    unsigned char pa[48], pb[48];
+};
+
+ElemTableB make_table_b(int ndim, int fclass) {
+    ElemTableB t;
+    memset(&t, 0, sizeof(t));
+    double xi[2], w[2];
+    sfem_gaussian_quadrature(-1, 1, 2, xi, w);
+    const int ox[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, oz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    const int ngp = ndim == 2 ? 4 : 8;
+    const int nen = fclass == SFEM_Q2 ? 9 : (1 << ndim);
+    for (int g = 0; g < ngp; ++g) {
+        double N[9], dN[27];
+        if (ndim == 2) {
+            t.w[g] = w[ox[g]] * w[oy[g]];
+            sfem_basis_function(2, fclass, xi[ox[g]], xi[oy[g]], 0.0, N, dN);
+        } else {
+            t.w[g] = w[ox[g]] * w[oy[g]] * w[oz[g]];
+            sfem_basis_function(3, fclass, xi[ox[g]], xi[oy[g]], xi[oz[g]], N, dN);
+        }
+        for (int a = 0; a < nen; ++a)
+            for (int k = 0; k < ndim; ++k) t.dN[g][a][k] = dN[k * nen + a];
+    }
+    int p = 0;
+    for (int a = 0; a < nen; ++a)
+        for (int b = a; b < nen; ++b) {
+            t.pa[p] = (unsigned char)a;
+            t.pb[p] = (unsigned char)b;
+            ++p;
+        }
+    return t;
+}
+
+struct BatchArgs {
+    const BatchMesh *meshes;
+    const int *order;
+    int64_t nmesh;
+    unsigned *queue;
+    // combined mesh
+    const double *X;
+    const int *ien;
+    int64_t nEl;
+    const int64_t *n2e_ptr;
+    const int *n2e;
+    const int *rowlen;
+    const int64_t *sliceptr;
+    const int *col;
+    const int *g2i;
+    const int *id;   // [b][nN] combined global DOF (0-based) of (node, comp); null for b == 1
+    int64_t nN, n_global;
+    // material and boundary data
+    const double *E;
+    int64_t nE;      // 1, nmesh or nEl (combined)
+    const double *nu;
+    int64_t nNu;
+    int plane;
+    const int64_t *fix_dofs;  // mesh-local, 1-based
+    const double *fix_vals;
+    // buffers
+    double *kbuf, *val64;
+    float *val32;
+    unsigned char *fixed, *gfixed;
+    double *ud, *b64, *x64, *q64;
+    void *vecT;      // x, r, z, p, q (type T, nd each) then minv (nN * b * b)
+    int64_t nd;
+    double *u_out;
+    // solver
+    double rtol, delta2;
+    int maxit, block_jacobi;
+    sfem_batch_stats *stats;
+    DevErr *err;
+};
+
+// Internal index (node*B + comp) of the mesh-local DOF gl (0-based), or -1
+// when no element uses it.  Scalar meshes have no ID: DOF = node.
+template <int B>
+__device__ __forceinline__ int local_to_internal(const BatchArgs &a, const BatchMesh &M, int64_t gl) {
+    const int64_t g = B == 1 ? M.node0 + gl : M.dof0 + gl;
+    return g < a.n_global ? a.g2i[g] : -1;
+}
+
+// Output position (global DOF of u) of internal DOF (node, comp).
+template <int B>
+__device__ __forceinline__ int64_t internal_to_output(const BatchArgs &a, const BatchMesh &M, int64_t node, int comp) {
+    return B == 1 ? M.dof0 + (node - M.node0) : (int64_t)a.id[(int64_t)comp * a.nN + node];
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// CTA-wide sums of (a, b) in a fixed order, returned to every thread.
+__device__ double2 block_sum2(double a, double b, double *sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    a = warp_sum_d(a);
+    b = warp_sum_d(b);
+    if (lane == 0) {
+        sh[warp] = a;
+        sh[32 + warp] = b;
+    }
+    __syncthreads();
+    double x = 0.0, y = 0.0;
+    for (int w = 0; w < nw; ++w) {
+        x += sh[w];
+        y += sh[32 + w];
+    }
+    __syncthreads();
+    return make_double2(x, y);
+}
+
+// y = (mask ? 0 : K x) over the mesh's slices; returns this thread's x.y share.
+// Rows at or beyond `rend` (the padding that rounds a mesh up to whole
+// slices) are neither written nor counted: their vector entries are unset.
+template <typename T, int B>
+__device__ double cta_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val,
+                           int64_t s0, int64_t s1, int64_t rend, const T *__restrict__ x, T *__restrict__ y,
+                           const unsigned char *__restrict__ fixed, bool masked) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double dot = 0.0;
+    for (int64_t s = s0 + warp; s < s1; s += nw) {
+        const int64_t r = s * 32 + lane;
+        const int64_t k0 = sliceptr[s], k1 = sliceptr[s + 1];
+        T acc[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) acc[i] = T(0);
+#pragma unroll 2
+        for (int64_t k = k0; k < k1; ++k) {
+            const int c = col[k * 32 + lane];
+            T v[B * B];
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) v[e] = val[(k * B * B + e) * 32 + lane];
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) acc[i] = fma(v[i * B + j], x[(int64_t)c * B + j], acc[i]);
+        }
+        if (r < rend) {
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                const int64_t d = r * B + i;
+                const T out = (masked && fixed[d]) ? T(0) : acc[i];
+                y[d] = out;
+                dot += (double)x[d] * (double)out;
+            }
+        }
+    }
+    return dot;
+}
+
+template <int NDIM, int NEN, int NGP, int B, bool MIXED>
+__global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
+    using T = typename std::conditional<MIXED, float, double>::type;
+    constexpr int GS = NEN * NDIM + 1;
+    constexpr int NPAIR = NEN * (NEN + 1) / 2;
+    extern __shared__ double smem[];
+    __shared__ double red[64];
+    __shared__ int s_mesh, s_flag;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const int ngroups = nw / NGP;  // element groups of NGP warps
+    const int grp = warp / NGP, gp = warp % NGP;
+    double *sG = smem + (int64_t)grp * (NGP * 32 * GS + NGP * 32);
+    double *sW = sG + NGP * 32 * GS;
+    T *xv = (T *)a.vecT;
+    T *rv = xv + a.nd, *zv = rv + a.nd, *pv = zv + a.nd, *qv = pv + a.nd;
+    T *minv = qv + a.nd;  // [nN][B][B]
+    const T *valT = MIXED ? (const T *)a.val32 : (const T *)a.val64;
+
+    for (;;) {
+        if (tid == 0) s_mesh = (int)atomicAdd(a.queue, 1u);
+        __syncthreads();
+        const int64_t q = s_mesh;
+        __syncthreads();
+        if (q >= a.nmesh) break;
+        const int mb = a.order[q];
+        const BatchMesh M = a.meshes[mb];
+        const int64_t n0 = M.node0, n1 = M.node0 + M.nnode;      // real nodes
+        const int64_t d0 = n0 * B, d1 = (M.node0 + ((M.nnode + 31) / 32) * 32) * B;  // padded DOF range
+
+        // ---- 1. element stiffness (FP64), NGP warps per group of 32 elements
+        const int64_t nel = M.elem1 - M.elem0;
+        const int64_t rounds = (nel + 32 * ngroups - 1) / (32 * ngroups);
+        for (int64_t rd = 0; rd < rounds; ++rd) {
+            const int64_t e = M.elem0 + (rd * ngroups + grp) * 32 + lane;
+            const bool live = grp < ngroups && e < M.elem1;
+            if (live) {
+                double xe[NEN][NDIM];
+#pragma unroll
+                for (int an = 0; an < NEN; ++an) {
+                    const int node = a.ien[(int64_t)an * a.nEl + e];
+#pragma unroll
+                    for (int i = 0; i < NDIM; ++i) xe[an][i] = a.X[(int64_t)node * NDIM + i];
+                }
+                double J[NDIM][NDIM];
+#pragma unroll
+                for (int i = 0; i < NDIM; ++i)
+#pragma unroll
+                    for (int k = 0; k < NDIM; ++k) {
+                        double s = 0.0;
+#pragma unroll
+                        for (int an = 0; an < NEN; ++an) s = fma(xe[an][i], tab.dN[gp][an][k], s);
+                        J[i][k] = s;
+                    }
+                double det, inv[NDIM][NDIM];
+                if (NDIM == 2) {
+                    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+                    const double r = 1.0 / det;
+                    inv[0][0] = J[1][1] * r;
+                    inv[0][1] = -J[0][1] * r;
+                    inv[1][0] = -J[1][0] * r;
+                    inv[1][1] = J[0][0] * r;
+                } else {
+                    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+                    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+                    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+                    det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+                    const double r = 1.0 / det;
+                    inv[0][0] = c00 * r;
+                    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+                    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+                    inv[1][0] = c01 * r;
+                    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+                    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+                    inv[2][0] = c02 * r;
+                    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+                    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+                }
+                if (det == 0.0) sfem_dev_error(a.err, SFEM_SINGULAR_JACOBIAN, e);
+                double *g = sG + ((int64_t)gp * 32 + lane) * GS;
+#pragma unroll
+                for (int an = 0; an < NEN; ++an)
+#pragma unroll
+                    for (int k = 0; k < NDIM; ++k) {
+                        double s = 0.0;
+#pragma unroll
+                        for (int j = 0; j < NDIM; ++j) s = fma(tab.dN[gp][an][j], inv[j][k], s);
+                        g[an * NDIM + k] = s;
+                    }
+                sW[gp * 32 + lane] = tab.w[gp] * fabs(det);
+            }
+            __syncthreads();
+            if (live) {
+                double lam = 0.0, mu = 0.0;
+                if (B > 1) {
+                    const int64_t iE = a.nE == 1 ? 0 : (a.nE == a.nmesh ? mb : e);
+                    const int64_t iN = a.nNu == 1 ? 0 : (a.nNu == a.nmesh ? mb : e);
+                    const double E = a.E[iE], nu = a.nu[iN];
+                    if (NDIM == 2 && a.plane == SFEM_PLANE_STRESS) {
+                        lam = nu * E / (1 - nu * nu);
+                        mu = E / (2 * (1 + nu));
+                    } else {
+                        const double c = E / ((1 + nu) * (1 - 2 * nu));
+                        lam = nu * c;
+                        mu = (1 - 2 * nu) / 2 * c;
+                    }
+                }
+                for (int p = gp; p < NPAIR; p += NGP) {
+                    const int pa = tab.pa[p], pb = tab.pb[p];
+                    if (B == 1) {
+                        double s = 0.0;
+#pragma unroll
+                        for (int qg = 0; qg < NGP; ++qg) {
+                            const double *g = sG + ((int64_t)qg * 32 + lane) * GS;
+                            double dd = 0.0;
+#pragma unroll
+                            for (int k = 0; k < NDIM; ++k) dd = fma(g[pa * NDIM + k], g[pb * NDIM + k], dd);
+                            s = fma(sW[qg * 32 + lane], dd, s);
+                        }
+                        a.kbuf[(int64_t)p * a.nEl + e] = s;
+                    } else {
+                        double S[NDIM][NDIM];
+#pragma unroll
+                        for (int i = 0; i < NDIM; ++i)
+#pragma unroll
+                            for (int j = 0; j < NDIM; ++j) S[i][j] = 0.0;
+#pragma unroll
+                        for (int qg = 0; qg < NGP; ++qg) {
+                            const double *g = sG + ((int64_t)qg * 32 + lane) * GS;
+                            const double wq = sW[qg * 32 + lane];
+#pragma unroll
+                            for (int i = 0; i < NDIM; ++i) {
+                                const double wa = wq * g[pa * NDIM + i];
+#pragma unroll
+                                for (int j = 0; j < NDIM; ++j) S[i][j] = fma(wa, g[pb * NDIM + j], S[i][j]);
+                            }
+                        }
+                        if (pa == pb) {
+#pragma unroll
+                            for (int i = 0; i < NDIM; ++i)
+#pragma unroll
+                                for (int j = 0; j < i; ++j) S[i][j] = S[j][i];
+                        }
+                        double tr = 0.0;
+#pragma unroll
+                        for (int i = 0; i < NDIM; ++i) tr += S[i][i];
+#pragma unroll
+                        for (int i = 0; i < NDIM; ++i)
+#pragma unroll
+                            for (int j = 0; j < NDIM; ++j) {
+                                double v = lam * S[i][j] + mu * S[j][i];
+                                if (i == j) v += mu * tr;
+                                a.kbuf[((int64_t)p * B * B + i * B + j) * a.nEl + e] = v;
+                            }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- 2. gather into the mesh's K blocks (ascending element order)
+        for (int64_t s = M.slice0 + warp; s < M.slice1; s += nw) {
+            const int64_t r64 = s * 32 + lane;
+            const int r = (int)r64;
+            const bool liver = r64 < a.nN;
+            const int64_t slab0 = a.sliceptr[s], width = a.sliceptr[s + 1] - slab0;
+            const int len = liver ? a.rowlen[r] : 0;
+            const int64_t q0 = liver ? a.n2e_ptr[r] : 0, q1 = liver ? a.n2e_ptr[r + 1] : 0;
+            for (int64_t k = 0; k < width; ++k) {
+                const int64_t slab = slab0 + k;
+                double acc[B * B];
+#pragma unroll
+                for (int i = 0; i < B * B; ++i) acc[i] = 0.0;
+                if (k < len) {
+                    const int c = a.col[slab * 32 + lane];
+                    int prev = -1;
+                    for (int64_t qq = q0; qq < q1; ++qq) {
+                        const int e = a.n2e[qq];
+                        if (e == prev) continue;
+                        prev = e;
+                        int nodes[NEN];
+#pragma unroll
+                        for (int an = 0; an < NEN; ++an) nodes[an] = a.ien[(int64_t)an * a.nEl + e];
+#pragma unroll
+                        for (int an = 0; an < NEN; ++an) {
+                            if (nodes[an] != r) continue;
+#pragma unroll
+                            for (int bq = 0; bq < NEN; ++bq) {
+                                if (nodes[bq] != c) continue;
+                                if (an <= bq) {
+                                    const int64_t base = (int64_t)sfem_pair(an, bq, NEN) * B * B;
+#pragma unroll
+                                    for (int i = 0; i < B * B; ++i) acc[i] += a.kbuf[(base + i) * a.nEl + e];
+                                } else {
+                                    const int64_t base = (int64_t)sfem_pair(bq, an, NEN) * B * B;
+#pragma unroll
+                                    for (int i = 0; i < B; ++i)
+#pragma unroll
+                                        for (int j = 0; j < B; ++j)
+                                            acc[i * B + j] += a.kbuf[(base + j * B + i) * a.nEl + e];
+                                }
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < B * B; ++i) {
+                    a.val64[(slab * B * B + i) * 32 + lane] = acc[i];
+                    if (MIXED) a.val32[(slab * B * B + i) * 32 + lane] = (float)acc[i];
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- 3. Dirichlet set-up
+        if (tid == 0) s_flag = SFEM_OK;
+        for (int64_t d = d0 + tid; d < d1; d += blockDim.x) {
+            const int64_t node = d / B;
+            a.fixed[d] = (node >= n1 || a.rowlen[node] == 0) ? 1 : 0;
+            a.ud[d] = 0.0;
+            a.x64[d] = 0.0;
+            xv[d] = T(0);
+        }
+        for (int64_t g = M.dof0 + tid; g < M.dof0 + M.ndof; g += blockDim.x) a.gfixed[g] = 0;
+        __syncthreads();
+        for (int64_t t = M.fix0 + tid; t < M.fix1; t += blockDim.x) {
+            const int64_t gl = a.fix_dofs[t] - 1;
+            if (gl < 0 || gl >= M.ndof) {
+                s_flag = SFEM_BAD_INDEX;
+                continue;
+            }
+            a.gfixed[M.dof0 + gl] = 1;
+            const int i = local_to_internal<B>(a, M, gl);
+            if (i >= 0) {
+                a.fixed[i] = 1;
+                a.ud[i] = a.fix_vals[t];
+            }
+        }
+        __syncthreads();
+        for (int64_t gl = tid; gl < M.ndof; gl += blockDim.x) {
+            if (local_to_internal<B>(a, M, gl) < 0 && !a.gfixed[M.dof0 + gl])
+                s_flag = SFEM_SINGULAR;  // a free DOF with no row in K
+        }
+        // b = -K q_d on the free DOFs (FP64)
+        cta_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0, M.slice1, n1, a.ud, a.q64, a.fixed, false);
+        __syncthreads();
+        for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) a.b64[d] = a.fixed[d] ? 0.0 : -a.q64[d];
+
+        // ---- 4. preconditioner: inverse of each node's free-restricted diagonal block
+        for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+            double D[B][B];
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) D[i][j] = 0.0;
+            const int len = a.rowlen[node];
+            const int64_t slab0 = a.sliceptr[node >> 5];
+            const int ln = (int)(node & 31);
+            for (int k = 0; k < len; ++k)
+                if (a.col[(slab0 + k) * 32 + ln] == (int)node) {
+#pragma unroll
+                    for (int i = 0; i < B; ++i)
+#pragma unroll
+                        for (int j = 0; j < B; ++j) D[i][j] = a.val64[((slab0 + k) * B * B + i * B + j) * 32 + ln];
+                    break;
+                }
+            bool fx[B];
+#pragma unroll
+            for (int i = 0; i < B; ++i) fx[i] = a.fixed[node * B + i] != 0;
+            double I[B][B];
+            bool bad = false;
+            if (B == 1 || !a.block_jacobi) {
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) I[i][j] = 0.0;
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+                    if (!fx[i]) {
+                        if (!(D[i][i] != 0.0)) bad = true;
+                        else I[i][i] = 1.0 / D[i][i];
+                    }
+            } else {
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j)
+                        if (fx[i] || fx[j]) D[i][j] = (i == j) ? 1.0 : 0.0;
+                double det;
+                if (B == 2) {
+                    det = D[0][0] * D[1][1] - D[0][1] * D[1][0];
+                    I[0][0] = D[1][1];
+                    I[0][1] = -D[0][1];
+                    I[1][0] = -D[1][0];
+                    I[1][1] = D[0][0];
+                } else {
+                    I[0][0] = D[1][1] * D[2][2] - D[1][2] * D[2][1];
+                    I[0][1] = D[0][2] * D[2][1] - D[0][1] * D[2][2];
+                    I[0][2] = D[0][1] * D[1][2] - D[0][2] * D[1][1];
+                    I[1][0] = D[1][2] * D[2][0] - D[1][0] * D[2][2];
+                    I[1][1] = D[0][0] * D[2][2] - D[0][2] * D[2][0];
+                    I[1][2] = D[0][2] * D[1][0] - D[0][0] * D[1][2];
+                    I[2][0] = D[1][0] * D[2][1] - D[1][1] * D[2][0];
+                    I[2][1] = D[0][1] * D[2][0] - D[0][0] * D[2][1];
+                    I[2][2] = D[0][0] * D[1][1] - D[0][1] * D[1][0];
+                    det = D[0][0] * I[0][0] + D[0][1] * I[1][0] + D[0][2] * I[2][0];
+                }
+                if (!(det != 0.0)) bad = true;
+                const double rd = det != 0.0 ? 1.0 / det : 0.0;
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) I[i][j] = (fx[i] || fx[j]) ? 0.0 : I[i][j] * rd;
+            }
+            if (bad) s_flag = SFEM_SINGULAR;
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) minv[(node * B + i) * B + j] = (T)I[i][j];
+        }
+        __syncthreads();
+
+        // ---- 5. preconditioned CG
+        double rz = 0.0, bb = 0.0;
+        {
+            double prz = 0.0, pbb = 0.0;
+            for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+                T r[B];
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    const double bv = a.b64[node * B + i];
+                    r[i] = (T)bv;
+                    rv[node * B + i] = r[i];
+                    pv[node * B + i] = T(0);
+                    pbb += bv * bv;
+                }
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    T zi = T(0);
+#pragma unroll
+                    for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
+                    zv[node * B + i] = zi;
+                    prz += (double)(r[i] * zi);
+                }
+            }
+            const double2 t = block_sum2(prz, pbb, red);
+            rz = t.x;
+            bb = t.y;
+        }
+        const double tol2 = a.rtol * a.rtol * bb;
+        double rr_ref = bb, rr = bb, beta = 0.0;
+        int it = 0, refreshes = 0, status = s_flag;
+        bool done = status != SFEM_OK || !(bb > 0.0);
+        while (!done) {
+            // p = z + beta p
+            for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) pv[d] = fma((T)beta, pv[d], zv[d]);
+            __syncthreads();
+            double pq = cta_spmv<T, B>(a.sliceptr, a.col, valT, M.slice0, M.slice1, n1, pv, qv, a.fixed, true);
+            pq = block_sum2(pq, 0.0, red).x;
+            if (!(pq > 0.0)) {
+                status = SFEM_SINGULAR;
+                break;
+            }
+            const T alpha = (T)(rz / pq);
+            double prz = 0.0, prr = 0.0;
+            for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+                T r[B];
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    const int64_t d = node * B + i;
+                    xv[d] = fma(alpha, pv[d], xv[d]);
+                    r[i] = fma(-alpha, qv[d], rv[d]);
+                    rv[d] = r[i];
+                    prr += (double)(r[i] * r[i]);
+                }
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    T zi = T(0);
+#pragma unroll
+                    for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
+                    zv[node * B + i] = zi;
+                    prz += (double)(r[i] * zi);
+                }
+            }
+            const double2 t = block_sum2(prz, prr, red);
+            ++it;
+            const double rz_prev = rz;
+            rz = t.x;
+            rr = t.y;
+            beta = rz_prev != 0.0 ? rz / rz_prev : 0.0;
+            if (!(rr == rr)) {
+                status = SFEM_SINGULAR;
+                break;
+            }
+            const bool at_tol = rr <= tol2, at_max = it >= a.maxit;
+            if (!MIXED) {
+                if (at_tol) break;
+                if (at_max) {
+                    status = SFEM_NOT_CONVERGED;
+                    break;
+                }
+                continue;
+            }
+            if (at_tol || at_max || rr <= a.delta2 * rr_ref) {
+                // FP64 refresh: fold the FP32 iterate, recompute r = b - K x in FP64
+                for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) {
+                    a.x64[d] += (double)xv[d];
+                    xv[d] = T(0);
+                }
+                __syncthreads();
+                cta_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0, M.slice1, n1, a.x64, a.q64, a.fixed,
+                                    true);
+                __syncthreads();
+                double frz = 0.0, frr = 0.0;
+                for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+                    T r[B];
+#pragma unroll
+                    for (int i = 0; i < B; ++i) {
+                        const int64_t d = node * B + i;
+                        const double v = a.fixed[d] ? 0.0 : a.b64[d] - a.q64[d];
+                        r[i] = (T)v;
+                        rv[d] = r[i];
+                        frr += v * v;
+                    }
+#pragma unroll
+                    for (int i = 0; i < B; ++i) {
+                        T zi = T(0);
+#pragma unroll
+                        for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
+                        zv[node * B + i] = zi;
+                        frz += (double)(r[i] * zi);
+                    }
+                }
+                const double2 f = block_sum2(frz, frr, red);
+                ++refreshes;
+                rz = f.x;
+                rr = f.y;
+                rr_ref = rr;
+                beta = rz_prev != 0.0 ? rz / rz_prev : 0.0;
+                if (rr <= tol2) break;
+                if (at_max) {
+                    status = SFEM_NOT_CONVERGED;
+                    break;
+                }
+            }
+        }
+        if (!MIXED && status != SFEM_SINGULAR) {
+            for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) a.x64[d] = (double)xv[d];
+        }
+        __syncthreads();
+
+        // ---- 6. u = q_d + x in the mesh's DOF numbering
+        for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+            if (a.rowlen[node] == 0) continue;
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                const int64_t g = internal_to_output<B>(a, M, node, i);
+                if (g >= 0) a.u_out[g] = a.ud[node * B + i] + a.x64[node * B + i];
+            }
+        }
+        for (int64_t t = M.fix0 + tid; t < M.fix1; t += blockDim.x) {  // prescribed DOFs outside K
+            const int64_t gl = a.fix_dofs[t] - 1;
+            if (gl < 0 || gl >= M.ndof) continue;
+            if (local_to_internal<B>(a, M, gl) < 0) a.u_out[M.dof0 + gl] = a.fix_vals[t];
+        }
+        if (tid == 0) {
+            sfem_batch_stats st;
+            st.status = status;
+            st.iterations = it;
+            st.refreshes = refreshes;
+            st.reserved = 0;
+            st.relres = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+            a.stats[mb] = st;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_batch_nodes(const double *__restrict__ Xin, const int64_t *__restrict__ IDin, int64_t total_nodes,
+                              const int64_t *__restrict__ node_off, const int64_t *__restrict__ pad_base,
+                              int64_t nmesh, int ndim, int b, double *__restrict__ Xc, int64_t *__restrict__ IDc,
+                              int64_t total_pad, DevErr *err) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total_pad) return;
+    int64_t lo = 0, hi = nmesh - 1;  // mesh with pad_base[m] <= t < pad_base[m+1]
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (pad_base[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t m = lo, local = t - pad_base[m], nn = node_off[m + 1] - node_off[m];
+    if (local < nn) {
+        const int64_t src = node_off[m] + local;
+        for (int i = 0; i < ndim; ++i) Xc[t * ndim + i] = Xin[src * ndim + i];
+        for (int d = 0; d < b; ++d) {
+            int64_t v = IDin ? IDin[(int64_t)d * total_nodes + src] : (int64_t)b * local + d + 1;
+            if (v < 1 || v > (int64_t)b * nn) {
+                sfem_dev_error(err, SFEM_BAD_INDEX, src);
+                v = 1;
+            }
+            IDc[(int64_t)d * total_pad + t] = (int64_t)b * node_off[m] + v;
+        }
+    } else {
+        for (int i = 0; i < ndim; ++i) Xc[t * ndim + i] = 0.0;
+        for (int d = 0; d < b; ++d) IDc[(int64_t)d * total_pad + t] = 0;  // never referenced
+    }
+}
+
+__global__ void k_batch_elems(const int64_t *__restrict__ IENin, int64_t total_el, int nen,
+                              const int64_t *__restrict__ elem_off, const int64_t *__restrict__ node_off,
+                              const int64_t *__restrict__ pad_base, int64_t nmesh, int64_t *__restrict__ IENc,
+                              DevErr *err) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total_el * nen) return;
+    const int64_t e = t % total_el;
+    int64_t lo = 0, hi = nmesh - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (elem_off[mid] <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t nn = node_off[lo + 1] - node_off[lo];
+    int64_t v = IENin[t];
+    if (v < 1 || v > nn) {
+        sfem_dev_error(err, SFEM_BAD_INDEX, e);
+        v = 1;
+    }
+    IENc[t] = pad_base[lo] + v;  // 1-based combined node id
+}
+
+template <int NDIM, int NEN, int NGP, int B, bool MIXED>
+int launch_batch(sfem_ctx *ctx, sfem_batch *bt, const BatchArgs &args) {
+    constexpr int GS = NEN * NDIM + 1;
+    const int threads = bt->threads;
+    const int ngroups = (threads / 32) / NGP;
+    const size_t smem = sizeof(double) * (size_t)ngroups * (NGP * 32 * GS + NGP * 32);
+    auto kern = k_batch<NDIM, NEN, NGP, B, MIXED>;
+    SFEM_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    SFEM_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    if (per_sm < 1) return sfem_set_error(ctx, SFEM_UNSUPPORTED, "batch kernel does not fit with %d threads", threads);
+    const int ctas = std::min<int64_t>((int64_t)std::min(per_sm, bt->ctas_per_sm) * ctx->num_sms, bt->nmesh);
+    const ElemTableB tab = make_table_b(NDIM, bt->fclass);
+    SFEM_CUDA(ctx, cudaMemsetAsync(bt->queue, 0, sizeof(unsigned), ctx->stream));
+    kern<<<std::max(ctas, 1), threads, smem, ctx->stream>>>(tab, args);
+    SFEM_LAUNCHED(ctx);
+    return sfem_cuda_status(ctx, cudaGetLastError(), "batch kernel launch");
+}
+
+template <bool MIXED>
+int dispatch_batch(sfem_ctx *ctx, sfem_batch *bt, const BatchArgs &args) {
+    if (bt->fclass == SFEM_Q2) return launch_batch<2, 9, 4, 1, MIXED>(ctx, bt, args);
+    if (bt->ndim == 2)
+        return bt->b == 1 ? launch_batch<2, 4, 4, 1, MIXED>(ctx, bt, args) : launch_batch<2, 4, 4, 2, MIXED>(ctx, bt, args);
+    return bt->b == 1 ? launch_batch<3, 8, 8, 1, MIXED>(ctx, bt, args) : launch_batch<3, 8, 8, 3, MIXED>(ctx, bt, args);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" int sfem_batch_create(sfem_ctx *ctx, int ndim, int function_class, int nDof, int64_t nmesh,
+                                 const int64_t *node_offsets, const int64_t *elem_offsets, const double *NodeList,
+                                 const int64_t *IEN, const int64_t *ID, int mem_space, sfem_batch **out) {
+    if (!ctx || !out || !node_offsets || !elem_offsets || nmesh < 1) return SFEM_BAD_ARG;
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    if (ndim != 2 && ndim != 3) return sfem_set_error(ctx, ndim == 1 ? SFEM_UNSUPPORTED : SFEM_BAD_ARG, "ndim must be 2 or 3");
+    if (nDof != 1 && nDof != ndim) return sfem_set_error(ctx, SFEM_UNSUPPORTED, "nDof must be 1 or ndim");
+    if (function_class == SFEM_Q2 && (ndim != 2 || nDof != 1))
+        return sfem_set_error(ctx, SFEM_UNSUPPORTED, "Q2 batches are 2D scalar only");
+    const int nen = function_class == SFEM_Q2 ? 9 : (1 << ndim);
+    sfem_batch *bt = new sfem_batch();
+    bt->ctx = ctx;
+    bt->ndim = ndim;
+    bt->nen = nen;
+    bt->b = nDof;
+    bt->fclass = function_class;
+    bt->nmesh = nmesh;
+    bt->h_node_off.resize(nmesh + 1);
+    bt->h_elem_off.resize(nmesh + 1);
+    bt->h_pad_base.resize(nmesh + 1);
+    int st = SFEM_OK;
+    int64_t *d_no = nullptr, *d_eo = nullptr, *d_pb = nullptr, *IDin = nullptr, *IENin = nullptr, *IDc = nullptr,
+            *IENc = nullptr;
+    double *Xin = nullptr, *Xc = nullptr;
+    do {
+        if ((st = sfem_check_ptr(ctx, node_offsets, mem_space)) || (st = sfem_check_ptr(ctx, elem_offsets, mem_space)))
+            break;
+        SFEM_CUDA(ctx, cudaMemcpy(bt->h_node_off.data(), node_offsets, sizeof(int64_t) * (nmesh + 1), cudaMemcpyDefault));
+        SFEM_CUDA(ctx, cudaMemcpy(bt->h_elem_off.data(), elem_offsets, sizeof(int64_t) * (nmesh + 1), cudaMemcpyDefault));
+        const auto &no = bt->h_node_off, &eo = bt->h_elem_off;
+        if (no[0] != 0 || eo[0] != 0) {
+            st = sfem_set_error(ctx, SFEM_BAD_ARG, "offsets must start at 0");
+            break;
+        }
+        bt->h_pad_base[0] = 0;
+        for (int64_t m = 0; m < nmesh; ++m) {
+            if (no[m + 1] <= no[m] || eo[m + 1] < eo[m]) {
+                st = sfem_set_error(ctx, SFEM_BAD_ARG, "mesh %lld has no nodes or negative elements", (long long)m);
+                break;
+            }
+            bt->h_pad_base[m + 1] = bt->h_pad_base[m] + sfem_cdiv(no[m + 1] - no[m], 32) * 32;
+        }
+        if (st) break;
+        bt->total_nodes = no[nmesh];
+        bt->total_elems = eo[nmesh];
+        bt->total_dofs = nDof * bt->total_nodes;
+        const int64_t total_pad = bt->h_pad_base[nmesh];
+        if (total_pad * nDof > INT_MAX / 2 || bt->total_elems * nen > INT_MAX) {
+            st = sfem_set_error(ctx, SFEM_BAD_ARG, "batch too large");
+            break;
+        }
+        const int64_t tn = bt->total_nodes, te = bt->total_elems;
+        if ((st = sfem_dalloc(ctx, (void **)&d_no, sizeof(int64_t) * (nmesh + 1), "offsets"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&d_eo, sizeof(int64_t) * (nmesh + 1), "offsets"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&d_pb, sizeof(int64_t) * (nmesh + 1), "offsets"))) break;
+        if ((st = sfem_copy_in(ctx, d_no, no.data(), sizeof(int64_t) * (nmesh + 1), SFEM_MEM_HOST))) break;
+        if ((st = sfem_copy_in(ctx, d_eo, eo.data(), sizeof(int64_t) * (nmesh + 1), SFEM_MEM_HOST))) break;
+        if ((st = sfem_copy_in(ctx, d_pb, bt->h_pad_base.data(), sizeof(int64_t) * (nmesh + 1), SFEM_MEM_HOST))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&Xin, sizeof(double) * ndim * tn, "NodeList"))) break;
+        if ((st = sfem_copy_in(ctx, Xin, NodeList, sizeof(double) * ndim * tn, mem_space))) break;
+        if (ID) {
+            if ((st = sfem_dalloc(ctx, (void **)&IDin, sizeof(int64_t) * nDof * tn, "ID"))) break;
+            if ((st = sfem_copy_in(ctx, IDin, ID, sizeof(int64_t) * nDof * tn, mem_space))) break;
+        }
+        if ((st = sfem_dalloc(ctx, (void **)&IENin, sizeof(int64_t) * (te * nen + 1), "IEN"))) break;
+        if ((st = sfem_copy_in(ctx, IENin, IEN, sizeof(int64_t) * te * nen, mem_space))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&Xc, sizeof(double) * ndim * total_pad, "combined nodes"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&IDc, sizeof(int64_t) * nDof * total_pad, "combined ID"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&IENc, sizeof(int64_t) * (te * nen + 1), "combined IEN"))) break;
+        k_batch_nodes<<<(unsigned)sfem_cdiv(total_pad, 256), 256, 0, ctx->stream>>>(
+            Xin, IDin, tn, d_no, d_pb, nmesh, ndim, nDof, Xc, IDc, total_pad, ctx->d_err);
+        SFEM_LAUNCHED(ctx);
+        if (te > 0) {
+            k_batch_elems<<<(unsigned)sfem_cdiv(te * nen, 256), 256, 0, ctx->stream>>>(IENin, te, nen, d_eo, d_no, d_pb,
+                                                                                     nmesh, IENc, ctx->d_err);
+            SFEM_LAUNCHED(ctx);
+        }
+        if ((st = sfem_check_device(ctx, "batch inputs"))) break;
+        if ((st = sfem_mesh_create_nel(ctx, ndim, function_class, nDof, te, Xc, total_pad, IENc, te, nen, IDc,
+                                       SFEM_MEM_DEVICE, &bt->mesh)))
+            break;
+        if ((st = sfem_pattern_build(ctx, bt->mesh, nullptr, nullptr))) break;
+        // per-mesh descriptors and the largest-first order
+        std::vector<BatchMesh> hm(nmesh);
+        std::vector<int> order(nmesh);
+        for (int64_t m = 0; m < nmesh; ++m) {
+            BatchMesh &M = hm[m];
+            M.node0 = bt->h_pad_base[m];
+            M.nnode = no[m + 1] - no[m];
+            M.slice0 = bt->h_pad_base[m] / 32;
+            M.slice1 = bt->h_pad_base[m + 1] / 32;
+            M.elem0 = eo[m];
+            M.elem1 = eo[m + 1];
+            M.dof0 = nDof * no[m];
+            M.ndof = nDof * M.nnode;
+            M.fix0 = M.fix1 = 0;
+            order[m] = (int)m;
+        }
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return hm[x].elem1 - hm[x].elem0 > hm[y].elem1 - hm[y].elem0; });
+        if ((st = sfem_dalloc(ctx, (void **)&bt->meshes, sizeof(BatchMesh) * nmesh, "batch meshes"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&bt->order, sizeof(int) * nmesh, "batch order"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&bt->queue, sizeof(unsigned), "batch queue"))) break;
+        if ((st = sfem_copy_in(ctx, bt->meshes, hm.data(), sizeof(BatchMesh) * nmesh, SFEM_MEM_HOST))) break;
+        if ((st = sfem_copy_in(ctx, bt->order, order.data(), sizeof(int) * nmesh, SFEM_MEM_HOST))) break;
+        st = sfem_check_device(ctx, "batch create");
+    } while (0);
+    void *tmp[] = {d_no, d_eo, d_pb, IDin, IENin, IDc, IENc, Xin, Xc};
+    for (void *p : tmp) sfem_dfree(ctx, p);
+    cudaStreamSynchronize(ctx->stream);
+    if (st != SFEM_OK) {
+        sfem_batch_destroy(bt);
+        return st;
+    }
+    *out = bt;
+    return SFEM_OK;
+}
+
+extern "C" int sfem_batch_info(const sfem_batch *bt, int64_t *total_dofs, int64_t *total_nodes,
+                               int64_t *total_elements) {
+    if (!bt) return SFEM_BAD_ARG;
+    if (total_dofs) *total_dofs = bt->total_dofs;
+    if (total_nodes) *total_nodes = bt->total_nodes;
+    if (total_elements) *total_elements = bt->total_elems;
+    return SFEM_OK;
+}
+
+extern "C" int sfem_batch_set_launch(sfem_batch *bt, int threads, int ctas_per_sm) {
+    if (!bt || (threads != 256 && threads != 512) || ctas_per_sm < 1 || ctas_per_sm > 8)
+        return SFEM_BAD_ARG;
+    const int ngp = bt->ndim == 2 ? 4 : 8;
+    if ((threads / 32) < ngp) return SFEM_BAD_ARG;
+    bt->threads = threads;
+    bt->ctas_per_sm = ctas_per_sm;
+    return SFEM_OK;
+}
+
+static int batch_buffers(sfem_ctx *ctx, sfem_batch *bt) {
+    if (bt->buffers) return SFEM_OK;
+    sfem_mesh *m = bt->mesh;
+    const int b = bt->b;
+    const int64_t nd = m->nN * b, nv = m->nslabs * 32 * b * b;
+    const int64_t nk = (int64_t)sfem_npairs(m->nen) * b * b * m->nEl;
+    const size_t tsz = sizeof(double);  // vecT sized for the FP64 variant (FP32 fits too)
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->kbuf, sizeof(double) * (nk + 1), "batch element stiffness"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->val64, sizeof(double) * (nv + 1), "batch K"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->val32, sizeof(float) * (nv + 1), "batch K fp32"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->ud, sizeof(double) * nd, "batch q_d"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->b64, sizeof(double) * nd, "batch rhs"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->x64, sizeof(double) * nd, "batch x"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->q64, sizeof(double) * nd, "batch q64"));
+    SFEM_TRY(sfem_dalloc(ctx, &bt->vecT, tsz * (5 * nd + m->nN * b * b), "batch CG vectors"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->fixed, nd, "batch mask"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->gfixed, bt->total_dofs + 1, "batch global mask"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->u, sizeof(double) * (bt->total_dofs + 1), "batch u"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->fix_off_dev, sizeof(int64_t) * (bt->nmesh + 1), "batch fix offsets"));
+    bt->buffers = true;
+    return SFEM_OK;
+}
+
+static int grow(sfem_ctx *ctx, void **p, int64_t *cap, int64_t need, size_t elem, const char *what) {
+    if (need <= *cap && *p) return SFEM_OK;
+    sfem_dfree(ctx, *p);
+    *p = nullptr;
+    SFEM_TRY(sfem_dalloc(ctx, p, elem * (need > 0 ? need : 1), what));
+    *cap = need;
+    return SFEM_OK;
+}
+
+extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *Young, int64_t nYoung,
+                                const double *nu, int64_t nNu, const int64_t *fix_offsets, const int64_t *fixed_dofs,
+                                const double *fixed_vals, double *u_out, int mem_space, const sfem_solve_opts *opts,
+                                sfem_batch_stats *stats) {
+    if (!ctx || !bt || !u_out || !fix_offsets) return SFEM_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    sfem_solve_opts o;
+    sfem_solve_opts_default(&o);
+    if (opts) o = *opts;
+    if (!(o.rtol >= 0.0) || o.maxit < 0 || (o.precision != SFEM_FP64 && o.precision != SFEM_MIXED) ||
+        !(o.reliable_delta > 0.0 && o.reliable_delta < 1.0))
+        return sfem_set_error(ctx, SFEM_BAD_ARG, "bad solve options");
+    if (plane != SFEM_PLANE_STRESS && plane != SFEM_PLANE_STRAIN) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad plane");
+    const int64_t nm = bt->nmesh;
+    if (bt->b > 1) {
+        if (!Young || !nu) return sfem_set_error(ctx, SFEM_BAD_ARG, "Young and nu are required for elasticity");
+        auto okn = [&](int64_t n) { return n == 1 || n == nm || n == bt->total_elems; };
+        if (!okn(nYoung) || !okn(nNu))
+            return sfem_set_error(ctx, SFEM_BAD_ARG, "Young/nu: length 1, nmesh or total elements");
+    } else {
+        nYoung = nNu = 1;
+    }
+    SFEM_TRY(sfem_check_ptr(ctx, fix_offsets, mem_space));
+    std::vector<int64_t> fo(nm + 1);
+    SFEM_CUDA(ctx, cudaMemcpy(fo.data(), fix_offsets, sizeof(int64_t) * (nm + 1), cudaMemcpyDefault));
+    if (fo[0] != 0) return sfem_set_error(ctx, SFEM_BAD_ARG, "fix_offsets must start at 0");
+    for (int64_t m = 0; m < nm; ++m)
+        if (fo[m + 1] < fo[m]) return sfem_set_error(ctx, SFEM_BAD_ARG, "fix_offsets must not decrease");
+    const int64_t nfix = fo[nm];
+    SFEM_TRY(batch_buffers(ctx, bt));
+    SFEM_TRY(grow(ctx, (void **)&bt->E, &bt->cap_E, nYoung, sizeof(double), "batch Young"));
+    SFEM_TRY(grow(ctx, (void **)&bt->nu, &bt->cap_nu, nNu, sizeof(double), "batch nu"));
+    SFEM_TRY(grow(ctx, (void **)&bt->fdofs, &bt->cap_fixd, nfix, sizeof(int64_t), "batch fixed dofs"));
+    SFEM_TRY(grow(ctx, (void **)&bt->fvals, &bt->cap_fixv, nfix, sizeof(double), "batch fixed values"));
+    if (bt->b > 1) {
+        SFEM_TRY(sfem_copy_in(ctx, bt->E, Young, sizeof(double) * nYoung, mem_space));
+        SFEM_TRY(sfem_copy_in(ctx, bt->nu, nu, sizeof(double) * nNu, mem_space));
+    }
+    SFEM_TRY(sfem_copy_in(ctx, bt->fdofs, fixed_dofs, sizeof(int64_t) * nfix, mem_space));
+    SFEM_TRY(sfem_copy_in(ctx, bt->fvals, fixed_vals, sizeof(double) * nfix, mem_space));
+    // fixed-DOF ranges into the per-mesh descriptors
+    {
+        std::vector<BatchMesh> hm(nm);
+        SFEM_CUDA(ctx, cudaMemcpyAsync(hm.data(), bt->meshes, sizeof(BatchMesh) * nm, cudaMemcpyDeviceToHost, ctx->stream));
+        SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int64_t m = 0; m < nm; ++m) {
+            hm[m].fix0 = fo[m];
+            hm[m].fix1 = fo[m + 1];
+        }
+        SFEM_CUDA(ctx, cudaMemcpyAsync(bt->meshes, hm.data(), sizeof(BatchMesh) * nm, cudaMemcpyHostToDevice, ctx->stream));
+        SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    sfem_batch_stats *dstats = nullptr;
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&dstats, sizeof(sfem_batch_stats) * nm, "batch stats"));
+    SFEM_CUDA(ctx, cudaMemsetAsync(bt->u, 0, sizeof(double) * (bt->total_dofs + 1), ctx->stream));
+    sfem_mesh *m = bt->mesh;
+    BatchArgs a;
+    memset(&a, 0, sizeof(a));
+    a.meshes = bt->meshes;
+    a.order = bt->order;
+    a.nmesh = nm;
+    a.queue = bt->queue;
+    a.X = m->X;
+    a.ien = m->ien;
+    a.nEl = m->nEl;
+    a.n2e_ptr = m->n2e_ptr;
+    a.n2e = m->n2e;
+    a.rowlen = m->rowlen;
+    a.sliceptr = m->sliceptr;
+    a.col = m->col;
+    a.g2i = m->g2i;
+    a.id = m->id;
+    a.nN = m->nN;
+    a.n_global = m->n_global;
+    a.E = bt->E;
+    a.nE = nYoung;
+    a.nu = bt->nu;
+    a.nNu = nNu;
+    a.plane = plane;
+    a.fix_dofs = bt->fdofs;
+    a.fix_vals = bt->fvals;
+    a.kbuf = bt->kbuf;
+    a.val64 = bt->val64;
+    a.val32 = bt->val32;
+    a.fixed = bt->fixed;
+    a.gfixed = bt->gfixed;
+    a.ud = bt->ud;
+    a.b64 = bt->b64;
+    a.x64 = bt->x64;
+    a.q64 = bt->q64;
+    a.vecT = bt->vecT;
+    a.nd = m->nN * bt->b;
+    a.u_out = bt->u;
+    a.rtol = o.rtol;
+    a.delta2 = o.reliable_delta * o.reliable_delta;
+    a.maxit = o.maxit > 0 ? o.maxit : 1000000;
+    a.block_jacobi = o.precond == SFEM_PC_BLOCK_JACOBI ? 1 : 0;
+    a.stats = dstats;
+    a.err = ctx->d_err;
+    int st = o.precision == SFEM_MIXED ? dispatch_batch<true>(ctx, bt, a) : dispatch_batch<false>(ctx, bt, a);
+    if (st == SFEM_OK) st = sfem_copy_out(ctx, u_out, bt->u, sizeof(double) * bt->total_dofs, mem_space);
+    if (st == SFEM_OK && stats)
+        st = sfem_cuda_status(ctx, cudaMemcpyAsync(stats, dstats, sizeof(sfem_batch_stats) * nm, cudaMemcpyDefault,
+                                                   ctx->stream),
+                              "stats copy");
+    if (st == SFEM_OK) st = sfem_check_device(ctx, "batch solve");
+    sfem_dfree(ctx, dstats);
+    cudaStreamSynchronize(ctx->stream);
+    return st;
+}
+
+extern "C" int sfem_batch_destroy(sfem_batch *bt) {
+    if (!bt) return SFEM_OK;
+    sfem_ctx *ctx = bt->ctx;
+    cudaSetDevice(ctx->device);
+    void *bufs[] = {bt->meshes, bt->order, bt->queue, bt->kbuf, bt->val64, bt->val32, bt->ud, bt->b64, bt->x64,
+                    bt->q64, bt->vecT, bt->fixed, bt->gfixed, bt->E, bt->nu, bt->fvals, bt->u, bt->fdofs,
+                    bt->fix_off_dev};
+    for (void *p : bufs) sfem_dfree(ctx, p);
+    if (bt->mesh) sfem_mesh_release(bt->mesh);
+    cudaStreamSynchronize(ctx->stream);
+    delete bt;
+    return SFEM_OK;
+}

@@ -96,6 +96,10 @@ int sfem_copy_out(sfem_ctx *ctx, void *dst, const void *src, size_t bytes, int m
 int sfem_scan_i32(sfem_ctx *ctx, const int *in, int64_t *out, int64_t n);
 int sfem_scan_i64(sfem_ctx *ctx, const int64_t *in, int64_t *out, int64_t n);
 void sfem_mesh_release(sfem_mesh *m);
+// sfem_mesh_create with an explicit element count (batches concatenate meshes).
+int sfem_mesh_create_nel(sfem_ctx *ctx, int ndim, int function_class, int nDof, int64_t nEl,
+                         const double *NodeList, int64_t nNodes, const int64_t *IEN, int64_t ldIEN, int nen,
+                         const int64_t *ID, int mem_space, sfem_mesh **out);
 
 #define SFEM_TRY(...)                     \
     do {                                  \

@@ -249,6 +249,22 @@ extern "C" int sfem_mesh_create(sfem_ctx *ctx, int ndim, int function_class, int
                                 int64_t ldIEN, int nen, const int64_t *ID, int mem_space,
                                 sfem_mesh **out) {
     if (!ctx || !out) return SFEM_BAD_ARG;
+    if (ne < 0) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad ne");
+    double nel_d = pow((double)ne, (double)ndim);
+    if (ndim >= 2 && ndim <= 3 && nel_d * nen > (double)INT_MAX)
+        return sfem_set_error(ctx, SFEM_BAD_ARG, "mesh too large (nEl*nen >= 2^31)");
+    int64_t nEl = 1;
+    for (int d = 0; d < ndim && ndim <= 3; ++d) nEl *= ne;  // src/fem.jl:179: elements 1:ne^ndim
+    int st = sfem_mesh_create_nel(ctx, ndim, function_class, nDof, nEl, NodeList, nNodes, IEN, ldIEN, nen, ID,
+                                  mem_space, out);
+    if (st == SFEM_OK) (*out)->ne = ne;
+    return st;
+}
+
+int sfem_mesh_create_nel(sfem_ctx *ctx, int ndim, int function_class, int nDof, int64_t nEl,
+                         const double *NodeList, int64_t nNodes, const int64_t *IEN, int64_t ldIEN, int nen,
+                         const int64_t *ID, int mem_space, sfem_mesh **out) {
+    if (!ctx || !out) return SFEM_BAD_ARG;
     *out = nullptr;
     cudaSetDevice(ctx->device);
     if (ndim == 1)
@@ -271,11 +287,8 @@ extern "C" int sfem_mesh_create(sfem_ctx *ctx, int ndim, int function_class, int
     if (nDof != 1 && nDof != ndim)
         return sfem_set_error(ctx, SFEM_UNSUPPORTED, "vector assembly needs nDof == ndim (src/fem.jl:210-231)");
     if (nDof > 1 && !ID) return sfem_set_error(ctx, SFEM_BAD_ARG, "ID is required when nDof > 1");
-    if (ne < 0 || nNodes < 1 || nNodes > INT_MAX / 4) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad ne/nNodes");
-    double nel_d = pow((double)ne, (double)ndim);
-    if (nel_d * nen > (double)INT_MAX) return sfem_set_error(ctx, SFEM_BAD_ARG, "mesh too large (nEl*nen >= 2^31)");
-    int64_t nEl = 1;
-    for (int d = 0; d < ndim; ++d) nEl *= ne;
+    if (nEl < 0 || nNodes < 1 || nNodes > INT_MAX / 4) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad nEl/nNodes");
+    if ((double)nEl * nen > (double)INT_MAX) return sfem_set_error(ctx, SFEM_BAD_ARG, "mesh too large (nEl*nen >= 2^31)");
     if (nEl > ldIEN)
         return sfem_set_error(ctx, SFEM_BAD_INDEX, "IEN has %lld rows but ne^ndim = %lld elements are assembled",
                               (long long)ldIEN, (long long)nEl);
@@ -287,7 +300,7 @@ extern "C" int sfem_mesh_create(sfem_ctx *ctx, int ndim, int function_class, int
     m->nen = nen;
     m->fclass = function_class;
     m->b = nDof;
-    m->ne = ne;
+    m->ne = 0;
     m->nEl = nEl;
     m->nN = nNodes;
     int st = SFEM_OK;

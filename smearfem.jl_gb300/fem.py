@@ -314,6 +314,96 @@ class Matrix:
             pass
 
 
+def _solve_opts(precision="fp64", precond="jacobi", rtol=1e-10, maxit=100000, check_every=32,
+                reliable_delta=0.1, profile=False, fp32_storage="upper"):
+    opts = L.SolveOpts()
+    lib().sfem_solve_opts_default(C.byref(opts))
+    opts.precision = {"fp64": L.FP64, "mixed": L.MIXED}[precision]
+    opts.precond = {"jacobi": L.PC_JACOBI, "block_jacobi": L.PC_BLOCK_JACOBI}[precond]
+    opts.rtol = rtol
+    opts.maxit = maxit
+    opts.check_every = check_every
+    opts.reliable_delta = reliable_delta
+    opts.profile = 1 if profile else 0
+    opts.fp32_storage = {"upper": L.FP32_UPPER, "full": L.FP32_FULL}[fp32_storage]
+    return opts
+
+
+class Batch:
+    """Many independent meshes of one element class (sfem_batch_*).
+
+    ``meshes`` is a list of ``(NodeList, IEN)`` or ``(NodeList, IEN, ID)``
+    tuples in the reference's shapes with mesh-local 1-based indices.
+    Every mesh is assembled and solved by one persistent kernel launch.
+    """
+
+    def __init__(self, meshes, ndim, nDof, FunctionClass="Q1", ctx=None):
+        self.ctx = ctx or get_context()
+        self.ndim, self.nDof = int(ndim), int(nDof)
+        nn = [np.shape(m[0])[1] for m in meshes]
+        ne = [np.shape(m[1])[0] for m in meshes]
+        self.node_off = np.concatenate([[0], np.cumsum(nn)]).astype(np.int64)
+        self.elem_off = np.concatenate([[0], np.cumsum(ne)]).astype(np.int64)
+        X = np.concatenate([np.asarray(m[0], dtype=np.float64) for m in meshes], axis=1)
+        IEN = np.concatenate([np.asarray(m[1], dtype=np.int64) for m in meshes], axis=0)
+        has_id = self.nDof > 1 and all(len(m) > 2 and m[2] is not None for m in meshes)
+        ID = np.concatenate([np.asarray(m[2], dtype=np.int64) for m in meshes], axis=0) if has_id else None
+        Xb, Eb, Ib = _Buf(X, np.float64), _Buf(IEN, np.int64), _Buf(ID, np.int64)
+        fc = {"Q1": L.Q1, "Q2": L.Q2}[FunctionClass]
+        h = C.c_void_p()
+        check(lib().sfem_batch_create(self.ctx.h, self.ndim, fc, self.nDof, len(meshes),
+                                      self.node_off.ctypes.data, self.elem_off.ctypes.data, Xb.ptr,
+                                      Eb.ptr, Ib.ptr, L.MEM_HOST, C.byref(h)), self.ctx.h)
+        self.h = h
+        self.nmesh = len(meshes)
+        td = C.c_int64()
+        check(lib().sfem_batch_info(h, C.byref(td), None, None), self.ctx.h)
+        self.total_dofs = td.value
+
+    @classmethod
+    def from_problems(cls, problems, ctx=None):
+        p0 = problems[0]
+        return cls([(p.NodeList, p.IEN[: p.n_elem], p.ID) for p in problems], p0.ndim, p0.nDof,
+                   ctx=ctx)
+
+    def set_launch(self, threads, ctas_per_sm):
+        check(lib().sfem_batch_set_launch(self.h, int(threads), int(ctas_per_sm)), self.ctx.h)
+
+    def solve(self, Young, nu, fixed_dofs, fixed_vals, plane="stress", out=None, **kw):
+        """``fixed_dofs``/``fixed_vals``: lists (one array per mesh, 1-based local
+        DOFs).  ``Young``/``nu``: scalar, per-mesh or per-element arrays.
+        Returns ``(u, stats)`` with ``u`` the concatenated displacements (mesh m
+        starts at nDof*node_offsets[m]) and ``stats`` a list of dicts."""
+        fo = np.concatenate([[0], np.cumsum([len(f) for f in fixed_dofs])]).astype(np.int64)
+        fd = np.concatenate([np.asarray(f, dtype=np.int64) for f in fixed_dofs])
+        fv = np.concatenate([np.asarray(v, dtype=np.float64) for v in fixed_vals])
+        Y = np.ascontiguousarray(np.atleast_1d(np.asarray(Young, dtype=np.float64)).ravel())
+        V = np.ascontiguousarray(np.atleast_1d(np.asarray(nu, dtype=np.float64)).ravel())
+        u = np.empty(self.total_dofs) if out is None else out
+        stats = (L.BatchStats * self.nmesh)()
+        opts = _solve_opts(**kw)
+        check(lib().sfem_batch_solve(self.ctx.h, self.h, _plane(plane), Y.ctypes.data, Y.size,
+                                     V.ctypes.data, V.size, fo.ctypes.data, fd.ctypes.data,
+                                     fv.ctypes.data, u.ctypes.data, L.MEM_HOST, C.byref(opts),
+                                     stats), self.ctx.h)
+        return u, [{k: getattr(s, k) for k, _ in s._fields_} for s in stats]
+
+    def split(self, u):
+        return [u[self.nDof * self.node_off[m]: self.nDof * self.node_off[m + 1]]
+                for m in range(self.nmesh)]
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sfem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ---------------------------------------------------------------------------
 # reference-shaped entry points
 # ---------------------------------------------------------------------------
