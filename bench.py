@@ -58,6 +58,8 @@ def parse_args(argv=None):
     ap.add_argument("--legs", default="value,mixed,e2e,cpu,batch",
                     help="comma list of value,mixed,e2e,cpu,batch (profiling runs pick one)")
     ap.add_argument("--batch-count", type=int, default=1024, help="meshes in the batch leg")
+    ap.add_argument("--batch-rtol", type=float, default=1e-12,
+                    help="batch-leg relative residual (1e-12 keeps the error in u under 1e-8)")
     ap.add_argument("--no-extras", action="store_true", help="same as --legs value")
     a = ap.parse_args(argv)
     a.legs = {"value"} if a.no_extras else set(x.strip() for x in a.legs.split(",") if x.strip())
@@ -444,7 +446,16 @@ def batch_leg(args, pkg, ctx, stream, dist):
     t0 = time.perf_counter()
     bt = pkg.Batch.from_problems(probs, ctx=ctx)
     t_setup = time.perf_counter() - t0
-    rtol = 1e-8
+    # the workload states PCG to 1e-8; the metric needs 1e-8 error in u, which
+    # this stiff plane-strain family reaches at a 1e-12 relative residual
+    rtol = args.batch_rtol
+    t0 = time.perf_counter()
+    # tuning trials: full solves of a quarter of the meshes, taken evenly
+    # from the size order (capping iterations would hide what clusters buy on
+    # the largest meshes)
+    shape, tuned_ms = bt.autotune(1.0, nus, fixed, vals, plane="strain", precision="mixed",
+                                  precond="block_jacobi", rtol=rtol, sample=max(1, len(probs) // 4))
+    t_tune = time.perf_counter() - t0
 
     def run_batch():
         return bt.solve(1.0, nus, fixed, vals, plane="strain", precision="mixed",
@@ -485,7 +496,10 @@ def batch_leg(args, pkg, ctx, stream, dist):
     return {"workload": f"{len(probs)} plane-strain Q1 quad meshes, n ~ U{{16..256}}, mixed "
                         f"block-Jacobi PCG to {rtol:g}, one persistent launch",
             "n_dof_total": n_total, "value": value, "unit": UNIT, "ms_per_batch": ms,
-            "setup_s": t_setup, "statuses_ok": int(sum(s["status"] == 0 for s in st)),
+            "setup_s": t_setup, "autotune_s": t_tune, "launch": shape,
+            "statuses_ok": int(sum(s["status"] == 0 for s in st)),
+            "mesh_ms": {"median": float(np.median([s["ms"] for s in st])),
+                        "max": float(max(s["ms"] for s in st))},
             "iterations": {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())},
             "rel_err_max_sample": max(errs), "rel_err_reference": "FP64 PCG to 1e-13 on every "
             f"{max(1, len(probs) // 32)}th mesh",

@@ -233,9 +233,10 @@ typedef struct {
     int status;      /* sfem_status of this mesh's solve                    */
     int iterations;  /* CG iterations                                       */
     int refreshes;   /* FP64 residual refreshes (SFEM_MIXED)                */
-    int reserved;
+    int group_ctas;  /* CTAs that worked on the mesh (1, or the cluster)    */
     double relres;   /* relative residual at exit (FP64 true residual for
                         SFEM_MIXED, recursive residual for SFEM_FP64)        */
+    double ms;       /* GPU time from the mesh's start to its result        */
 } sfem_batch_stats;
 
 /* Upload nmesh meshes.  Mesh m owns nodes [node_offsets[m], node_offsets[m+1])
@@ -254,9 +255,12 @@ SFEM_API int sfem_batch_create(sfem_ctx *ctx, int ndim, int function_class, int 
 SFEM_API int sfem_batch_info(const sfem_batch *batch, int64_t *total_dofs, int64_t *total_nodes,
                              int64_t *total_elements);
 
-/* Launch shape of the persistent kernel: threads per CTA (256 or 512) and
- * CTAs per SM (capped by occupancy).  sfem_batch_autotune picks them. */
-SFEM_API int sfem_batch_set_launch(sfem_batch *batch, int threads, int ctas_per_sm);
+/* Launch shape of the persistent kernel: threads per CTA (256 or 512), CTAs
+ * per SM (capped by occupancy) and the thread-block cluster size (1, 2, 4, 8
+ * or 16) that works together on every mesh with at least cluster_min_nodes
+ * nodes; smaller meshes get one CTA each.  sfem_batch_autotune picks them. */
+SFEM_API int sfem_batch_set_launch(sfem_batch *batch, int threads, int ctas_per_sm, int cluster,
+                                   int64_t cluster_min_nodes);
 
 /* Assemble and solve every mesh in one persistent kernel launch.
  *   Young/nu: length 1 (all), nmesh (per mesh) or total elements.
@@ -273,6 +277,20 @@ SFEM_API int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *batch, int plane, const
                               const int64_t *fix_offsets, const int64_t *fixed_dofs,
                               const double *fixed_vals, double *u_out, int mem_space,
                               const sfem_solve_opts *opts, sfem_batch_stats *stats);
+/* Project autotuner for the persistent kernel's launch shape: runs the solve
+ * (same arguments as sfem_batch_solve) on a sample of about `sample` meshes
+ * taken evenly from the batch's size order, for a set of candidate shapes
+ * (threads per CTA, CTAs per SM, cluster size, cluster threshold), times each
+ * with CUDA events and keeps the fastest for later sfem_batch_solve calls.
+ * best_ms: time of the best candidate on the sample. */
+SFEM_API int sfem_batch_autotune(sfem_ctx *ctx, sfem_batch *batch, int plane, const double *Young,
+                                 int64_t nYoung, const double *nu, int64_t nNu,
+                                 const int64_t *fix_offsets, const int64_t *fixed_dofs,
+                                 const double *fixed_vals, int mem_space,
+                                 const sfem_solve_opts *opts, int64_t sample, double *best_ms);
+/* The launch shape in use, and the grid of the last launch. */
+SFEM_API int sfem_batch_get_launch(const sfem_batch *batch, int *threads, int *ctas_per_sm,
+                                   int *cluster, int64_t *cluster_min_nodes, int *last_grid);
 SFEM_API int sfem_batch_destroy(sfem_batch *batch);
 
 #ifdef __cplusplus

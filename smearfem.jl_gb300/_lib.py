@@ -50,7 +50,7 @@ class SolveStats(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("refreshes", C.c_int),
-                ("reserved", C.c_int), ("relres", C.c_double)]
+                ("group_ctas", C.c_int), ("relres", C.c_double), ("ms", C.c_double)]
 
 
 _lib = None
@@ -85,9 +85,13 @@ SIGNATURES = {
     "sfem_solve_opts_default": (None, [C.POINTER(SolveOpts)]),
     "sfem_batch_create": (C.c_int, [P, C.c_int, C.c_int, C.c_int, I64, P, P, P, P, P, C.c_int, PP]),
     "sfem_batch_info": (C.c_int, [P, I64P, I64P, I64P]),
-    "sfem_batch_set_launch": (C.c_int, [P, C.c_int, C.c_int]),
+    "sfem_batch_set_launch": (C.c_int, [P, C.c_int, C.c_int, C.c_int, I64]),
     "sfem_batch_solve": (C.c_int, [P, P, C.c_int, P, I64, P, I64, P, P, P, P, C.c_int,
                                    C.POINTER(SolveOpts), P]),
+    "sfem_batch_autotune": (C.c_int, [P, P, C.c_int, P, I64, P, I64, P, P, P, C.c_int,
+                                      C.POINTER(SolveOpts), I64, C.POINTER(C.c_double)]),
+    "sfem_batch_get_launch": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), I64P, C.POINTER(C.c_int)]),
     "sfem_batch_destroy": (C.c_int, [P]),
     "sfem_solve_dirichlet": (C.c_int, [P, P, P, I64, P, P, P, C.c_int, C.POINTER(SolveOpts),
                                        C.POINTER(SolveStats)]),

@@ -27,7 +27,11 @@
 #include <type_traits>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "sfem_internal.cuh"
+
+namespace cgrp = cooperative_groups;
 
 struct BatchMesh {
     int64_t node0, nnode;      // combined (padded) node range start, real node count
@@ -56,6 +60,10 @@ struct sfem_batch {
     int64_t *fdofs = nullptr, *fix_off_dev = nullptr;
     int64_t cap_E = 0, cap_nu = 0, cap_fixd = 0, cap_fixv = 0;
     int threads = 512, ctas_per_sm = 1;  // launch shape (autotuned)
+    int cluster = 4;                     // CTAs per cluster working on one large mesh
+    int64_t big_nodes = 16384;           // meshes with at least this many nodes use a cluster
+    int last_grid = 0, last_cluster = 0;
+    std::vector<int64_t> h_nodes;        // nodes per mesh
 };
 
 namespace {
@@ -98,9 +106,10 @@ ElemTableB make_table_b(int ndim, int fclass) {
 
 struct BatchArgs {
     const BatchMesh *meshes;
-    const int *order;
-    int64_t nmesh;
-    unsigned *queue;
+    const int *order;     // large meshes first (cluster work), then small ones
+    int64_t nmesh, nbig;  // meshes in `order`, of which the first nbig are large
+    int64_t nmesh_all;    // meshes in the batch (per-mesh material arrays)
+    unsigned *queue;      // [0]: next large mesh, [1]: next small mesh
     // combined mesh
     const double *X;
     const int *ien;
@@ -178,13 +187,14 @@ __device__ double2 block_sum2(double a, double b, double *sh) {
 // y = (mask ? 0 : K x) over the mesh's slices; returns this thread's x.y share.
 // Rows at or beyond `rend` (the padding that rounds a mesh up to whole
 // slices) are neither written nor counted: their vector entries are unset.
+// Slices sfirst, sfirst + sstride, ... below s1 (one warp each).
 template <typename T, int B>
-__device__ double cta_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val,
-                           int64_t s0, int64_t s1, int64_t rend, const T *__restrict__ x, T *__restrict__ y,
-                           const unsigned char *__restrict__ fixed, bool masked) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+__device__ double grp_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val,
+                           int64_t sfirst, int64_t s1, int64_t sstride, int64_t rend, const T *__restrict__ x,
+                           T *__restrict__ y, const unsigned char *__restrict__ fixed, bool masked) {
+    const int lane = threadIdx.x & 31;
     double dot = 0.0;
-    for (int64_t s = s0 + warp; s < s1; s += nw) {
+    for (int64_t s = sfirst; s < s1; s += sstride) {
         const int64_t r = s * 32 + lane;
         const int64_t k0 = sliceptr[s], k1 = sliceptr[s + 1];
         T acc[B];
@@ -214,15 +224,66 @@ __device__ double cta_spmv(const int64_t *__restrict__ sliceptr, const int *__re
     return dot;
 }
 
-template <int NDIM, int NEN, int NGP, int B, bool MIXED>
-__global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
+// One CTA working alone on a mesh.
+struct SoloGroup {
+    __device__ __forceinline__ int rank() const { return 0; }
+    __device__ __forceinline__ int size() const { return 1; }
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ double2 sum2(double a, double b, double *red, double *) const { return block_sum2(a, b, red); }
+    __device__ int max_flag(int *flag) const {
+        __syncthreads();
+        const int f = *flag;
+        __syncthreads();
+        return f;
+    }
+};
+
+// A thread-block cluster working together on a mesh: hardware cluster
+// barrier, partial sums exchanged through distributed shared memory and
+// added in rank order (deterministic).
+struct ClusterGroup {
+    __device__ __forceinline__ int rank() const { return (int)cgrp::this_cluster().block_rank(); }
+    __device__ __forceinline__ int size() const { return (int)cgrp::this_cluster().num_blocks(); }
+    __device__ __forceinline__ void sync() const { cgrp::this_cluster().sync(); }
+    __device__ double2 sum2(double a, double b, double *red, double *xch) const {
+        const double2 p = block_sum2(a, b, red);
+        cgrp::cluster_group cl = cgrp::this_cluster();
+        if (threadIdx.x == 0) {
+            xch[0] = p.x;
+            xch[1] = p.y;
+        }
+        cl.sync();
+        double x = 0.0, y = 0.0;
+        for (unsigned r = 0; r < cl.num_blocks(); ++r) {
+            const double *rx = cl.map_shared_rank(xch, r);
+            x += rx[0];
+            y += rx[1];
+        }
+        cl.sync();
+        return make_double2(x, y);
+    }
+    __device__ int max_flag(int *flag) const {
+        cgrp::cluster_group cl = cgrp::this_cluster();
+        cl.sync();
+        int f = 0;
+        for (unsigned r = 0; r < cl.num_blocks(); ++r) f = max(f, *cl.map_shared_rank(flag, r));
+        cl.sync();
+        return f;
+    }
+};
+
+// Assemble and solve mesh `mb` with group G (a CTA or a cluster).
+template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED>
+__device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
+                             int *s_flag) {
     using T = typename std::conditional<MIXED, float, double>::type;
     constexpr int GS = NEN * NDIM + 1;
     constexpr int NPAIR = NEN * (NEN + 1) / 2;
     extern __shared__ double smem[];
-    __shared__ double red[64];
-    __shared__ int s_mesh, s_flag;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const int grank = G.rank(), gsize = G.size();
+    const int64_t gt = (int64_t)grank * blockDim.x + tid, gstride = (int64_t)gsize * blockDim.x;
+    const int64_t gw = (int64_t)grank * nw + warp, gnw = (int64_t)gsize * nw;
     const int ngroups = nw / NGP;  // element groups of NGP warps
     const int grp = warp / NGP, gp = warp % NGP;
     double *sG = smem + (int64_t)grp * (NGP * 32 * GS + NGP * 32);
@@ -231,23 +292,18 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
     T *rv = xv + a.nd, *zv = rv + a.nd, *pv = zv + a.nd, *qv = pv + a.nd;
     T *minv = qv + a.nd;  // [nN][B][B]
     const T *valT = MIXED ? (const T *)a.val32 : (const T *)a.val64;
-
-    for (;;) {
-        if (tid == 0) s_mesh = (int)atomicAdd(a.queue, 1u);
-        __syncthreads();
-        const int64_t q = s_mesh;
-        __syncthreads();
-        if (q >= a.nmesh) break;
-        const int mb = a.order[q];
-        const BatchMesh M = a.meshes[mb];
+    const BatchMesh M = a.meshes[mb];
+    unsigned long long t_start = 0;
+    if (tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+    {
         const int64_t n0 = M.node0, n1 = M.node0 + M.nnode;      // real nodes
         const int64_t d0 = n0 * B, d1 = (M.node0 + ((M.nnode + 31) / 32) * 32) * B;  // padded DOF range
 
         // ---- 1. element stiffness (FP64), NGP warps per group of 32 elements
         const int64_t nel = M.elem1 - M.elem0;
-        const int64_t rounds = (nel + 32 * ngroups - 1) / (32 * ngroups);
+        const int64_t rounds = (nel + 32 * ngroups * gsize - 1) / (32 * ngroups * gsize);
         for (int64_t rd = 0; rd < rounds; ++rd) {
-            const int64_t e = M.elem0 + (rd * ngroups + grp) * 32 + lane;
+            const int64_t e = M.elem0 + ((rd * gsize + grank) * ngroups + grp) * 32 + lane;
             const bool live = grp < ngroups && e < M.elem1;
             if (live) {
                 double xe[NEN][NDIM];
@@ -308,8 +364,8 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
             if (live) {
                 double lam = 0.0, mu = 0.0;
                 if (B > 1) {
-                    const int64_t iE = a.nE == 1 ? 0 : (a.nE == a.nmesh ? mb : e);
-                    const int64_t iN = a.nNu == 1 ? 0 : (a.nNu == a.nmesh ? mb : e);
+                    const int64_t iE = a.nE == 1 ? 0 : (a.nE == a.nmesh_all ? mb : e);
+                    const int64_t iN = a.nNu == 1 ? 0 : (a.nNu == a.nmesh_all ? mb : e);
                     const double E = a.E[iE], nu = a.nu[iN];
                     if (NDIM == 2 && a.plane == SFEM_PLANE_STRESS) {
                         lam = nu * E / (1 - nu * nu);
@@ -373,8 +429,9 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
             __syncthreads();
         }
 
+        G.sync();  // every element block of the mesh is in kbuf
         // ---- 2. gather into the mesh's K blocks (ascending element order)
-        for (int64_t s = M.slice0 + warp; s < M.slice1; s += nw) {
+        for (int64_t s = M.slice0 + gw; s < M.slice1; s += gnw) {
             const int64_t r64 = s * 32 + lane;
             const int r = (int)r64;
             const bool liver = r64 < a.nN;
@@ -425,23 +482,23 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
                 }
             }
         }
-        __syncthreads();
+        if (tid == 0) *s_flag = SFEM_OK;
+        G.sync();
 
         // ---- 3. Dirichlet set-up
-        if (tid == 0) s_flag = SFEM_OK;
-        for (int64_t d = d0 + tid; d < d1; d += blockDim.x) {
+        for (int64_t d = d0 + gt; d < d1; d += gstride) {
             const int64_t node = d / B;
             a.fixed[d] = (node >= n1 || a.rowlen[node] == 0) ? 1 : 0;
             a.ud[d] = 0.0;
             a.x64[d] = 0.0;
             xv[d] = T(0);
         }
-        for (int64_t g = M.dof0 + tid; g < M.dof0 + M.ndof; g += blockDim.x) a.gfixed[g] = 0;
-        __syncthreads();
-        for (int64_t t = M.fix0 + tid; t < M.fix1; t += blockDim.x) {
+        for (int64_t g = M.dof0 + gt; g < M.dof0 + M.ndof; g += gstride) a.gfixed[g] = 0;
+        G.sync();
+        for (int64_t t = M.fix0 + gt; t < M.fix1; t += gstride) {
             const int64_t gl = a.fix_dofs[t] - 1;
             if (gl < 0 || gl >= M.ndof) {
-                s_flag = SFEM_BAD_INDEX;
+                atomicMax(s_flag, (int)SFEM_BAD_INDEX);
                 continue;
             }
             a.gfixed[M.dof0 + gl] = 1;
@@ -451,18 +508,18 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
                 a.ud[i] = a.fix_vals[t];
             }
         }
-        __syncthreads();
-        for (int64_t gl = tid; gl < M.ndof; gl += blockDim.x) {
+        G.sync();
+        for (int64_t gl = gt; gl < M.ndof; gl += gstride) {
             if (local_to_internal<B>(a, M, gl) < 0 && !a.gfixed[M.dof0 + gl])
-                s_flag = SFEM_SINGULAR;  // a free DOF with no row in K
+                atomicMax(s_flag, (int)SFEM_SINGULAR);  // a free DOF with no row in K
         }
         // b = -K q_d on the free DOFs (FP64)
-        cta_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0, M.slice1, n1, a.ud, a.q64, a.fixed, false);
-        __syncthreads();
-        for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) a.b64[d] = a.fixed[d] ? 0.0 : -a.q64[d];
+        grp_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.ud, a.q64, a.fixed, false);
+        G.sync();
+        for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) a.b64[d] = a.fixed[d] ? 0.0 : -a.q64[d];
 
         // ---- 4. preconditioner: inverse of each node's free-restricted diagonal block
-        for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+        for (int64_t node = n0 + gt; node < n1; node += gstride) {
             double D[B][B];
 #pragma unroll
             for (int i = 0; i < B; ++i)
@@ -527,19 +584,19 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
 #pragma unroll
                     for (int j = 0; j < B; ++j) I[i][j] = (fx[i] || fx[j]) ? 0.0 : I[i][j] * rd;
             }
-            if (bad) s_flag = SFEM_SINGULAR;
+            if (bad) atomicMax(s_flag, (int)SFEM_SINGULAR);
 #pragma unroll
             for (int i = 0; i < B; ++i)
 #pragma unroll
                 for (int j = 0; j < B; ++j) minv[(node * B + i) * B + j] = (T)I[i][j];
         }
-        __syncthreads();
+        G.sync();
 
         // ---- 5. preconditioned CG
         double rz = 0.0, bb = 0.0;
         {
             double prz = 0.0, pbb = 0.0;
-            for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+            for (int64_t node = n0 + gt; node < n1; node += gstride) {
                 T r[B];
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
@@ -558,27 +615,27 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
                     prz += (double)(r[i] * zi);
                 }
             }
-            const double2 t = block_sum2(prz, pbb, red);
+            const double2 t = G.sum2(prz, pbb, red, xch);
             rz = t.x;
             bb = t.y;
         }
         const double tol2 = a.rtol * a.rtol * bb;
         double rr_ref = bb, rr = bb, beta = 0.0;
-        int it = 0, refreshes = 0, status = s_flag;
+        int it = 0, refreshes = 0, status = G.max_flag(s_flag);
         bool done = status != SFEM_OK || !(bb > 0.0);
         while (!done) {
             // p = z + beta p
-            for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) pv[d] = fma((T)beta, pv[d], zv[d]);
-            __syncthreads();
-            double pq = cta_spmv<T, B>(a.sliceptr, a.col, valT, M.slice0, M.slice1, n1, pv, qv, a.fixed, true);
-            pq = block_sum2(pq, 0.0, red).x;
+            for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) pv[d] = fma((T)beta, pv[d], zv[d]);
+            G.sync();
+            double pq = grp_spmv<T, B>(a.sliceptr, a.col, valT, M.slice0 + gw, M.slice1, gnw, n1, pv, qv, a.fixed, true);
+            pq = G.sum2(pq, 0.0, red, xch).x;
             if (!(pq > 0.0)) {
                 status = SFEM_SINGULAR;
                 break;
             }
             const T alpha = (T)(rz / pq);
             double prz = 0.0, prr = 0.0;
-            for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+            for (int64_t node = n0 + gt; node < n1; node += gstride) {
                 T r[B];
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
@@ -597,7 +654,7 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
                     prz += (double)(r[i] * zi);
                 }
             }
-            const double2 t = block_sum2(prz, prr, red);
+            const double2 t = G.sum2(prz, prr, red, xch);
             ++it;
             const double rz_prev = rz;
             rz = t.x;
@@ -618,16 +675,16 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
             }
             if (at_tol || at_max || rr <= a.delta2 * rr_ref) {
                 // FP64 refresh: fold the FP32 iterate, recompute r = b - K x in FP64
-                for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) {
+                for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) {
                     a.x64[d] += (double)xv[d];
                     xv[d] = T(0);
                 }
-                __syncthreads();
-                cta_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0, M.slice1, n1, a.x64, a.q64, a.fixed,
-                                    true);
-                __syncthreads();
+                G.sync();
+                grp_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.x64, a.q64,
+                                    a.fixed, true);
+                G.sync();
                 double frz = 0.0, frr = 0.0;
-                for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+                for (int64_t node = n0 + gt; node < n1; node += gstride) {
                     T r[B];
 #pragma unroll
                     for (int i = 0; i < B; ++i) {
@@ -646,7 +703,7 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
                         frz += (double)(r[i] * zi);
                     }
                 }
-                const double2 f = block_sum2(frz, frr, red);
+                const double2 f = G.sum2(frz, frr, red, xch);
                 ++refreshes;
                 rz = f.x;
                 rr = f.y;
@@ -660,12 +717,12 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
             }
         }
         if (!MIXED && status != SFEM_SINGULAR) {
-            for (int64_t d = n0 * B + tid; d < n1 * B; d += blockDim.x) a.x64[d] = (double)xv[d];
+            for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) a.x64[d] = (double)xv[d];
         }
-        __syncthreads();
+        G.sync();
 
         // ---- 6. u = q_d + x in the mesh's DOF numbering
-        for (int64_t node = n0 + tid; node < n1; node += blockDim.x) {
+        for (int64_t node = n0 + gt; node < n1; node += gstride) {
             if (a.rowlen[node] == 0) continue;
 #pragma unroll
             for (int i = 0; i < B; ++i) {
@@ -673,22 +730,56 @@ __global__ void __launch_bounds__(512) k_batch(const __grid_constant__ ElemTable
                 if (g >= 0) a.u_out[g] = a.ud[node * B + i] + a.x64[node * B + i];
             }
         }
-        for (int64_t t = M.fix0 + tid; t < M.fix1; t += blockDim.x) {  // prescribed DOFs outside K
+        for (int64_t t = M.fix0 + gt; t < M.fix1; t += gstride) {  // prescribed DOFs outside K
             const int64_t gl = a.fix_dofs[t] - 1;
             if (gl < 0 || gl >= M.ndof) continue;
             if (local_to_internal<B>(a, M, gl) < 0) a.u_out[M.dof0 + gl] = a.fix_vals[t];
         }
-        if (tid == 0) {
+        if (grank == 0 && tid == 0) {
+            unsigned long long t_end;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
             sfem_batch_stats st;
             st.status = status;
             st.iterations = it;
             st.refreshes = refreshes;
-            st.reserved = 0;
+            st.group_ctas = gsize;
             st.relres = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+            st.ms = (double)(t_end - t_start) * 1e-6;
             a.stats[mb] = st;
         }
+    }
+}
+
+// 2D classes fit two 512-thread CTAs per SM (64 registers); 3D elasticity
+// needs the full register file of one.
+template <int NDIM, int NEN, int NGP, int B, bool MIXED>
+__global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
+    __shared__ double red[64];
+    __shared__ double xch[2];
+    __shared__ int s_flag, s_mesh;
+    const int tid = threadIdx.x;
+    cgrp::cluster_group cl = cgrp::this_cluster();
+    // 1. large meshes: the whole cluster works on one mesh
+    for (;;) {
+        if (cl.block_rank() == 0 && tid == 0) s_mesh = (int)atomicAdd(a.queue, 1u);
+        cl.sync();
+        const int64_t q = *cl.map_shared_rank(&s_mesh, 0);
+        cl.sync();
+        if (q >= a.nbig) break;
+        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED>(ClusterGroup(), tab, a, a.order[q], red, xch, &s_flag);
+        cl.sync();
+    }
+    // 2. small meshes: every CTA on its own
+    for (;;) {
+        if (tid == 0) s_mesh = (int)atomicAdd(a.queue + 1, 1u);
+        __syncthreads();
+        const int64_t q = (int64_t)a.nbig + s_mesh;
+        __syncthreads();
+        if (q >= a.nmesh) break;
+        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED>(SoloGroup(), tab, a, a.order[q], red, xch, &s_flag);
         __syncthreads();
     }
+    cl.sync();  // peers may still read this CTA's shared memory until every CTA is done
 }
 
 __global__ void k_batch_nodes(const double *__restrict__ Xin, const int64_t *__restrict__ IDin, int64_t total_nodes,
@@ -751,13 +842,44 @@ int launch_batch(sfem_ctx *ctx, sfem_batch *bt, const BatchArgs &args) {
     const size_t smem = sizeof(double) * (size_t)ngroups * (NGP * 32 * GS + NGP * 32);
     auto kern = k_batch<NDIM, NEN, NGP, B, MIXED>;
     SFEM_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    SFEM_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
-    if (per_sm < 1) return sfem_set_error(ctx, SFEM_UNSUPPORTED, "batch kernel does not fit with %d threads", threads);
-    const int ctas = std::min<int64_t>((int64_t)std::min(per_sm, bt->ctas_per_sm) * ctx->num_sms, bt->nmesh);
     const ElemTableB tab = make_table_b(NDIM, bt->fclass);
-    SFEM_CUDA(ctx, cudaMemsetAsync(bt->queue, 0, sizeof(unsigned), ctx->stream));
-    kern<<<std::max(ctas, 1), threads, smem, ctx->stream>>>(tab, args);
+    SFEM_CUDA(ctx, cudaMemsetAsync(bt->queue, 0, 2 * sizeof(unsigned), ctx->stream));
+    int csize = bt->cluster;
+    int nclusters = 0;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchAttribute attr[1];
+    cfg.blockDim = dim3(threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    if (csize > 1) {
+        if (csize > 8) SFEM_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = csize;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(csize * ctx->num_sms, 1, 1);
+        if (cudaOccupancyMaxActiveClusters(&nclusters, (void *)kern, &cfg) != cudaSuccess || nclusters < 1) {
+            cudaGetLastError();
+            csize = 1;  // clusters of this shape do not fit: every CTA works alone
+        }
+    }
+    if (csize <= 1) {
+        int per_sm = 0;
+        SFEM_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+        if (per_sm < 1) return sfem_set_error(ctx, SFEM_UNSUPPORTED, "batch kernel does not fit with %d threads", threads);
+        nclusters = std::min(per_sm, bt->ctas_per_sm) * ctx->num_sms;
+        cfg.attrs = nullptr;
+        cfg.numAttrs = 0;
+        csize = 1;
+    }
+    const int64_t want = std::max<int64_t>(1, std::min<int64_t>((int64_t)nclusters * csize, bt->nmesh * csize));
+    cfg.gridDim = dim3((unsigned)(want / csize * csize), 1, 1);
+    bt->last_grid = (int)cfg.gridDim.x;
+    bt->last_cluster = csize;
+    SFEM_CUDA(ctx, cudaLaunchKernelEx(&cfg, kern, tab, args));
     SFEM_LAUNCHED(ctx);
     return sfem_cuda_status(ctx, cudaGetLastError(), "batch kernel launch");
 }
@@ -875,11 +997,12 @@ extern "C" int sfem_batch_create(sfem_ctx *ctx, int ndim, int function_class, in
             M.fix0 = M.fix1 = 0;
             order[m] = (int)m;
         }
-        std::stable_sort(order.begin(), order.end(),
-                         [&](int x, int y) { return hm[x].elem1 - hm[x].elem0 > hm[y].elem1 - hm[y].elem0; });
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return hm[x].nnode > hm[y].nnode; });
+        bt->h_nodes.resize(nmesh);
+        for (int64_t mm = 0; mm < nmesh; ++mm) bt->h_nodes[mm] = hm[order[mm]].nnode;  // in queue order
         if ((st = sfem_dalloc(ctx, (void **)&bt->meshes, sizeof(BatchMesh) * nmesh, "batch meshes"))) break;
         if ((st = sfem_dalloc(ctx, (void **)&bt->order, sizeof(int) * nmesh, "batch order"))) break;
-        if ((st = sfem_dalloc(ctx, (void **)&bt->queue, sizeof(unsigned), "batch queue"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&bt->queue, 2 * sizeof(unsigned), "batch queue"))) break;
         if ((st = sfem_copy_in(ctx, bt->meshes, hm.data(), sizeof(BatchMesh) * nmesh, SFEM_MEM_HOST))) break;
         if ((st = sfem_copy_in(ctx, bt->order, order.data(), sizeof(int) * nmesh, SFEM_MEM_HOST))) break;
         st = sfem_check_device(ctx, "batch create");
@@ -904,13 +1027,18 @@ extern "C" int sfem_batch_info(const sfem_batch *bt, int64_t *total_dofs, int64_
     return SFEM_OK;
 }
 
-extern "C" int sfem_batch_set_launch(sfem_batch *bt, int threads, int ctas_per_sm) {
+extern "C" int sfem_batch_set_launch(sfem_batch *bt, int threads, int ctas_per_sm, int cluster,
+                                     int64_t cluster_min_nodes) {
     if (!bt || (threads != 256 && threads != 512) || ctas_per_sm < 1 || ctas_per_sm > 8)
         return SFEM_BAD_ARG;
+    if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16) return SFEM_BAD_ARG;
+    if (cluster_min_nodes < 1) return SFEM_BAD_ARG;
     const int ngp = bt->ndim == 2 ? 4 : 8;
     if ((threads / 32) < ngp) return SFEM_BAD_ARG;
     bt->threads = threads;
     bt->ctas_per_sm = ctas_per_sm;
+    bt->cluster = cluster;
+    bt->big_nodes = cluster_min_nodes;
     return SFEM_OK;
 }
 
@@ -946,27 +1074,20 @@ static int grow(sfem_ctx *ctx, void **p, int64_t *cap, int64_t need, size_t elem
     return SFEM_OK;
 }
 
-extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *Young, int64_t nYoung,
-                                const double *nu, int64_t nNu, const int64_t *fix_offsets, const int64_t *fixed_dofs,
-                                const double *fixed_vals, double *u_out, int mem_space, const sfem_solve_opts *opts,
-                                sfem_batch_stats *stats) {
-    if (!ctx || !bt || !u_out || !fix_offsets) return SFEM_BAD_ARG;
-    cudaSetDevice(ctx->device);
-    sfem_solve_opts o;
-    sfem_solve_opts_default(&o);
-    if (opts) o = *opts;
-    if (!(o.rtol >= 0.0) || o.maxit < 0 || (o.precision != SFEM_FP64 && o.precision != SFEM_MIXED) ||
-        !(o.reliable_delta > 0.0 && o.reliable_delta < 1.0))
-        return sfem_set_error(ctx, SFEM_BAD_ARG, "bad solve options");
+// Copy material and boundary data into the batch's buffers and record each
+// mesh's fixed-DOF range.
+static int batch_upload(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *Young, int64_t *nYoung,
+                        const double *nu, int64_t *nNu, const int64_t *fix_offsets, const int64_t *fixed_dofs,
+                        const double *fixed_vals, int mem_space) {
     if (plane != SFEM_PLANE_STRESS && plane != SFEM_PLANE_STRAIN) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad plane");
     const int64_t nm = bt->nmesh;
     if (bt->b > 1) {
         if (!Young || !nu) return sfem_set_error(ctx, SFEM_BAD_ARG, "Young and nu are required for elasticity");
         auto okn = [&](int64_t n) { return n == 1 || n == nm || n == bt->total_elems; };
-        if (!okn(nYoung) || !okn(nNu))
+        if (!okn(*nYoung) || !okn(*nNu))
             return sfem_set_error(ctx, SFEM_BAD_ARG, "Young/nu: length 1, nmesh or total elements");
     } else {
-        nYoung = nNu = 1;
+        *nYoung = *nNu = 1;
     }
     SFEM_TRY(sfem_check_ptr(ctx, fix_offsets, mem_space));
     std::vector<int64_t> fo(nm + 1);
@@ -976,37 +1097,40 @@ extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const 
         if (fo[m + 1] < fo[m]) return sfem_set_error(ctx, SFEM_BAD_ARG, "fix_offsets must not decrease");
     const int64_t nfix = fo[nm];
     SFEM_TRY(batch_buffers(ctx, bt));
-    SFEM_TRY(grow(ctx, (void **)&bt->E, &bt->cap_E, nYoung, sizeof(double), "batch Young"));
-    SFEM_TRY(grow(ctx, (void **)&bt->nu, &bt->cap_nu, nNu, sizeof(double), "batch nu"));
+    SFEM_TRY(grow(ctx, (void **)&bt->E, &bt->cap_E, *nYoung, sizeof(double), "batch Young"));
+    SFEM_TRY(grow(ctx, (void **)&bt->nu, &bt->cap_nu, *nNu, sizeof(double), "batch nu"));
     SFEM_TRY(grow(ctx, (void **)&bt->fdofs, &bt->cap_fixd, nfix, sizeof(int64_t), "batch fixed dofs"));
     SFEM_TRY(grow(ctx, (void **)&bt->fvals, &bt->cap_fixv, nfix, sizeof(double), "batch fixed values"));
     if (bt->b > 1) {
-        SFEM_TRY(sfem_copy_in(ctx, bt->E, Young, sizeof(double) * nYoung, mem_space));
-        SFEM_TRY(sfem_copy_in(ctx, bt->nu, nu, sizeof(double) * nNu, mem_space));
+        SFEM_TRY(sfem_copy_in(ctx, bt->E, Young, sizeof(double) * *nYoung, mem_space));
+        SFEM_TRY(sfem_copy_in(ctx, bt->nu, nu, sizeof(double) * *nNu, mem_space));
     }
     SFEM_TRY(sfem_copy_in(ctx, bt->fdofs, fixed_dofs, sizeof(int64_t) * nfix, mem_space));
     SFEM_TRY(sfem_copy_in(ctx, bt->fvals, fixed_vals, sizeof(double) * nfix, mem_space));
-    // fixed-DOF ranges into the per-mesh descriptors
-    {
-        std::vector<BatchMesh> hm(nm);
-        SFEM_CUDA(ctx, cudaMemcpyAsync(hm.data(), bt->meshes, sizeof(BatchMesh) * nm, cudaMemcpyDeviceToHost, ctx->stream));
-        SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        for (int64_t m = 0; m < nm; ++m) {
-            hm[m].fix0 = fo[m];
-            hm[m].fix1 = fo[m + 1];
-        }
-        SFEM_CUDA(ctx, cudaMemcpyAsync(bt->meshes, hm.data(), sizeof(BatchMesh) * nm, cudaMemcpyHostToDevice, ctx->stream));
-        SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<BatchMesh> hm(nm);
+    SFEM_CUDA(ctx, cudaMemcpyAsync(hm.data(), bt->meshes, sizeof(BatchMesh) * nm, cudaMemcpyDeviceToHost, ctx->stream));
+    SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t m = 0; m < nm; ++m) {
+        hm[m].fix0 = fo[m];
+        hm[m].fix1 = fo[m + 1];
     }
-    sfem_batch_stats *dstats = nullptr;
-    SFEM_TRY(sfem_dalloc(ctx, (void **)&dstats, sizeof(sfem_batch_stats) * nm, "batch stats"));
-    SFEM_CUDA(ctx, cudaMemsetAsync(bt->u, 0, sizeof(double) * (bt->total_dofs + 1), ctx->stream));
+    SFEM_CUDA(ctx, cudaMemcpyAsync(bt->meshes, hm.data(), sizeof(BatchMesh) * nm, cudaMemcpyHostToDevice, ctx->stream));
+    return SFEM_OK;
+}
+
+// Launch the persistent kernel over the meshes order[0..n) (decreasing size;
+// `nodes` holds their node counts in the same order).
+static int batch_run(sfem_ctx *ctx, sfem_batch *bt, const sfem_solve_opts &o, int plane, int64_t nYoung,
+                     int64_t nNu, const int *order, int64_t n, const int64_t *nodes, sfem_batch_stats *dstats) {
     sfem_mesh *m = bt->mesh;
     BatchArgs a;
     memset(&a, 0, sizeof(a));
     a.meshes = bt->meshes;
-    a.order = bt->order;
-    a.nmesh = nm;
+    a.order = order;
+    a.nmesh = n;
+    a.nbig = 0;
+    if (bt->cluster > 1)
+        while (a.nbig < n && nodes[a.nbig] >= bt->big_nodes) ++a.nbig;
     a.queue = bt->queue;
     a.X = m->X;
     a.ien = m->ien;
@@ -1045,7 +1169,34 @@ extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const 
     a.block_jacobi = o.precond == SFEM_PC_BLOCK_JACOBI ? 1 : 0;
     a.stats = dstats;
     a.err = ctx->d_err;
-    int st = o.precision == SFEM_MIXED ? dispatch_batch<true>(ctx, bt, a) : dispatch_batch<false>(ctx, bt, a);
+    a.nmesh_all = bt->nmesh;
+    return o.precision == SFEM_MIXED ? dispatch_batch<true>(ctx, bt, a) : dispatch_batch<false>(ctx, bt, a);
+}
+
+static int batch_opts(sfem_ctx *ctx, const sfem_solve_opts *opts, sfem_solve_opts *o) {
+    sfem_solve_opts_default(o);
+    if (opts) *o = *opts;
+    if (!(o->rtol >= 0.0) || o->maxit < 0 || (o->precision != SFEM_FP64 && o->precision != SFEM_MIXED) ||
+        (o->precond != SFEM_PC_JACOBI && o->precond != SFEM_PC_BLOCK_JACOBI) ||
+        !(o->reliable_delta > 0.0 && o->reliable_delta < 1.0))
+        return sfem_set_error(ctx, SFEM_BAD_ARG, "bad solve options");
+    return SFEM_OK;
+}
+
+extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *Young, int64_t nYoung,
+                                const double *nu, int64_t nNu, const int64_t *fix_offsets, const int64_t *fixed_dofs,
+                                const double *fixed_vals, double *u_out, int mem_space, const sfem_solve_opts *opts,
+                                sfem_batch_stats *stats) {
+    if (!ctx || !bt || !u_out || !fix_offsets) return SFEM_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    sfem_solve_opts o;
+    SFEM_TRY(batch_opts(ctx, opts, &o));
+    SFEM_TRY(batch_upload(ctx, bt, plane, Young, &nYoung, nu, &nNu, fix_offsets, fixed_dofs, fixed_vals, mem_space));
+    const int64_t nm = bt->nmesh;
+    sfem_batch_stats *dstats = nullptr;
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&dstats, sizeof(sfem_batch_stats) * nm, "batch stats"));
+    SFEM_CUDA(ctx, cudaMemsetAsync(bt->u, 0, sizeof(double) * (bt->total_dofs + 1), ctx->stream));
+    int st = batch_run(ctx, bt, o, plane, nYoung, nNu, bt->order, nm, bt->h_nodes.data(), dstats);
     if (st == SFEM_OK) st = sfem_copy_out(ctx, u_out, bt->u, sizeof(double) * bt->total_dofs, mem_space);
     if (st == SFEM_OK && stats)
         st = sfem_cuda_status(ctx, cudaMemcpyAsync(stats, dstats, sizeof(sfem_batch_stats) * nm, cudaMemcpyDefault,
@@ -1055,6 +1206,85 @@ extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const 
     sfem_dfree(ctx, dstats);
     cudaStreamSynchronize(ctx->stream);
     return st;
+}
+
+// Autotuner: time candidate launch shapes on a sample of the batch (every
+// k-th mesh in size order, so the sample keeps the batch's size mix) and
+// keep the fastest.
+extern "C" int sfem_batch_autotune(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *Young, int64_t nYoung,
+                                   const double *nu, int64_t nNu, const int64_t *fix_offsets,
+                                   const int64_t *fixed_dofs, const double *fixed_vals, int mem_space,
+                                   const sfem_solve_opts *opts, int64_t sample, double *best_ms) {
+    if (!ctx || !bt || !fix_offsets) return SFEM_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    sfem_solve_opts o;
+    SFEM_TRY(batch_opts(ctx, opts, &o));
+    SFEM_TRY(batch_upload(ctx, bt, plane, Young, &nYoung, nu, &nNu, fix_offsets, fixed_dofs, fixed_vals, mem_space));
+    const int64_t nm = bt->nmesh;
+    const int64_t stride = std::max<int64_t>(1, sample > 0 ? nm / sample : 1);
+    std::vector<int> horder(nm);
+    SFEM_CUDA(ctx, cudaMemcpy(horder.data(), bt->order, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+    std::vector<int> sub;
+    std::vector<int64_t> subnodes;
+    for (int64_t q = 0; q < nm; q += stride) {
+        sub.push_back(horder[q]);
+        subnodes.push_back(bt->h_nodes[q]);
+    }
+    const int64_t ns = (int64_t)sub.size();
+    int *dsub = nullptr;
+    sfem_batch_stats *dstats = nullptr;
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&dsub, sizeof(int) * ns, "autotune order"));
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&dstats, sizeof(sfem_batch_stats) * nm, "autotune stats"));
+    SFEM_TRY(sfem_copy_in(ctx, dsub, sub.data(), sizeof(int) * ns, SFEM_MEM_HOST));
+    struct Cand { int threads, ctas, cluster; int64_t min_nodes; };
+    // Candidates span "every CTA on its own mesh" to clusters of 4 or 8 CTAs
+    // on the larger meshes (measured on GB300: 16-CTA clusters leave too few
+    // meshes in flight and lose).
+    const int64_t big = bt->ndim == 2 ? 16384 : 32768;
+    const Cand cands[] = {{512, 1, 1, big},     {512, 2, 1, big},     {512, 1, 4, big},
+                          {512, 1, 4, big / 4}, {512, 1, 8, big / 4}, {512, 1, 8, big},
+                          {256, 2, 4, big}};
+    const int nc = (int)(sizeof(cands) / sizeof(cands[0]));
+    cudaEvent_t e0, e1;
+    SFEM_CUDA(ctx, cudaEventCreate(&e0));
+    SFEM_CUDA(ctx, cudaEventCreate(&e1));
+    double best = 1e300;
+    Cand pick = {bt->threads, bt->ctas_per_sm, bt->cluster, bt->big_nodes};
+    int st = SFEM_OK;
+    for (int c = 0; c < nc && st == SFEM_OK; ++c) {
+        if (sfem_batch_set_launch(bt, cands[c].threads, cands[c].ctas, cands[c].cluster, cands[c].min_nodes) != SFEM_OK)
+            continue;
+        cudaEventRecord(e0, ctx->stream);
+        st = batch_run(ctx, bt, o, plane, nYoung, nNu, dsub, ns, subnodes.data(), dstats);
+        cudaEventRecord(e1, ctx->stream);
+        if (st != SFEM_OK) break;
+        SFEM_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            pick = cands[c];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sfem_dfree(ctx, dsub);
+    sfem_dfree(ctx, dstats);
+    sfem_batch_set_launch(bt, pick.threads, pick.ctas, pick.cluster, pick.min_nodes);
+    if (st == SFEM_OK) st = sfem_check_device(ctx, "batch autotune");
+    if (best_ms) *best_ms = best;
+    return st;
+}
+
+extern "C" int sfem_batch_get_launch(const sfem_batch *bt, int *threads, int *ctas_per_sm, int *cluster,
+                                     int64_t *cluster_min_nodes, int *last_grid) {
+    if (!bt) return SFEM_BAD_ARG;
+    if (threads) *threads = bt->threads;
+    if (ctas_per_sm) *ctas_per_sm = bt->ctas_per_sm;
+    if (cluster) *cluster = bt->cluster;
+    if (cluster_min_nodes) *cluster_min_nodes = bt->big_nodes;
+    if (last_grid) *last_grid = bt->last_grid;
+    return SFEM_OK;
 }
 
 extern "C" int sfem_batch_destroy(sfem_batch *bt) {

@@ -366,19 +366,44 @@ class Batch:
         return cls([(p.NodeList, p.IEN[: p.n_elem], p.ID) for p in problems], p0.ndim, p0.nDof,
                    ctx=ctx)
 
-    def set_launch(self, threads, ctas_per_sm):
-        check(lib().sfem_batch_set_launch(self.h, int(threads), int(ctas_per_sm)), self.ctx.h)
+    def set_launch(self, threads=512, ctas_per_sm=1, cluster=8, cluster_min_nodes=16384):
+        check(lib().sfem_batch_set_launch(self.h, int(threads), int(ctas_per_sm), int(cluster),
+                                          int(cluster_min_nodes)), self.ctx.h)
+
+    def _pack(self, Young, nu, fixed_dofs, fixed_vals):
+        fo = np.concatenate([[0], np.cumsum([len(f) for f in fixed_dofs])]).astype(np.int64)
+        fd = np.concatenate([np.asarray(f, dtype=np.int64) for f in fixed_dofs])
+        fv = np.concatenate([np.asarray(v, dtype=np.float64) for v in fixed_vals])
+        Y = np.ascontiguousarray(np.atleast_1d(np.asarray(Young, dtype=np.float64)).ravel())
+        V = np.ascontiguousarray(np.atleast_1d(np.asarray(nu, dtype=np.float64)).ravel())
+        return fo, fd, fv, Y, V
+
+    def autotune(self, Young, nu, fixed_dofs, fixed_vals, plane="stress", sample=128, **kw):
+        """Pick the persistent kernel's launch shape by timing candidates on a
+        sample of this batch; returns (launch shape dict, best sample ms)."""
+        fo, fd, fv, Y, V = self._pack(Young, nu, fixed_dofs, fixed_vals)
+        opts = _solve_opts(**kw)
+        best = C.c_double()
+        check(lib().sfem_batch_autotune(self.ctx.h, self.h, _plane(plane), Y.ctypes.data, Y.size,
+                                        V.ctypes.data, V.size, fo.ctypes.data, fd.ctypes.data,
+                                        fv.ctypes.data, L.MEM_HOST, C.byref(opts), int(sample),
+                                        C.byref(best)), self.ctx.h)
+        return self.launch(), best.value
+
+    def launch(self):
+        t, c, cl, grid = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        mn = C.c_int64()
+        check(lib().sfem_batch_get_launch(self.h, C.byref(t), C.byref(c), C.byref(cl), C.byref(mn),
+                                          C.byref(grid)), self.ctx.h)
+        return {"threads": t.value, "ctas_per_sm": c.value, "cluster": cl.value,
+                "cluster_min_nodes": mn.value, "last_grid": grid.value}
 
     def solve(self, Young, nu, fixed_dofs, fixed_vals, plane="stress", out=None, **kw):
         """``fixed_dofs``/``fixed_vals``: lists (one array per mesh, 1-based local
         DOFs).  ``Young``/``nu``: scalar, per-mesh or per-element arrays.
         Returns ``(u, stats)`` with ``u`` the concatenated displacements (mesh m
         starts at nDof*node_offsets[m]) and ``stats`` a list of dicts."""
-        fo = np.concatenate([[0], np.cumsum([len(f) for f in fixed_dofs])]).astype(np.int64)
-        fd = np.concatenate([np.asarray(f, dtype=np.int64) for f in fixed_dofs])
-        fv = np.concatenate([np.asarray(v, dtype=np.float64) for v in fixed_vals])
-        Y = np.ascontiguousarray(np.atleast_1d(np.asarray(Young, dtype=np.float64)).ravel())
-        V = np.ascontiguousarray(np.atleast_1d(np.asarray(nu, dtype=np.float64)).ravel())
+        fo, fd, fv, Y, V = self._pack(Young, nu, fixed_dofs, fixed_vals)
         u = np.empty(self.total_dofs) if out is None else out
         stats = (L.BatchStats * self.nmesh)()
         opts = _solve_opts(**kw)

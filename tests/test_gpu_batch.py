@@ -122,3 +122,59 @@ def test_batch_errors_and_status(sfem, ctx):
         IEN = IEN.copy()
         IEN[0, 0] = 99
         sfem.Batch([(NL, IEN, ID)], 2, 2, ctx=ctx)
+
+
+@pytest.mark.parametrize("cluster", [2, 8])
+def test_cluster_mode(sfem, ctx, cluster):
+    """Meshes solved by a thread-block cluster (forced for every mesh here)
+    match their single-mesh solves, and stay bitwise identical alone vs in
+    the mix for a fixed launch shape."""
+    probs = _quads([20, 9, 33, 5, 27], seed=31)
+
+    def run(ps):
+        bt = sfem.Batch.from_problems(ps, ctx=ctx)
+        bt.set_launch(512, 1, cluster, 1)
+        u, st = bt.solve(1.0, np.array([float(p.nu[0]) for p in ps]), [p.fixed_dofs for p in ps],
+                         [p.fixed_vals for p in ps], plane="strain", precision="mixed",
+                         precond="block_jacobi", rtol=1e-10)
+        parts = bt.split(u)
+        bt.close()
+        return parts, st
+
+    parts, st = run(probs)
+    for p, u, s in zip(probs, parts, st):
+        assert s["status"] == 0
+        assert _rel(u, _single(sfem, ctx, p)) <= TOL_U
+    alone, _ = run([probs[2]])
+    assert np.array_equal(alone[0], parts[2])
+
+
+def test_cluster_mode_3d_fp64(sfem, ctx):
+    mg = sfem.meshgen
+    probs = [mg.hex_problem(n, 70 + n, jitter=0.2, e_sigma=0.5, nu=0.3, top="modes", rtol=1e-10)
+             for n in (6, 4)]
+    bt = sfem.Batch.from_problems(probs, ctx=ctx)
+    bt.set_launch(256, 1, 4, 1)
+    E = np.concatenate([p.Young for p in probs])
+    u, st = bt.solve(E, 0.3, [p.fixed_dofs for p in probs], [p.fixed_vals for p in probs],
+                     precision="fp64", precond="block_jacobi", rtol=1e-11)
+    for p, up, s in zip(probs, bt.split(u), st):
+        assert s["status"] == 0
+        assert _rel(up, _single(sfem, ctx, p)) <= TOL_U
+    bt.close()
+
+
+def test_autotune_picks_a_valid_shape(sfem, ctx):
+    probs = _quads([30, 12, 70, 9, 44, 5], seed=51)
+    bt = sfem.Batch.from_problems(probs, ctx=ctx)
+    nus = np.array([float(p.nu[0]) for p in probs])
+    fx, fv = [p.fixed_dofs for p in probs], [p.fixed_vals for p in probs]
+    shape, ms = bt.autotune(1.0, nus, fx, fv, plane="strain", precision="mixed",
+                            precond="block_jacobi", rtol=1e-10, sample=6)
+    assert ms > 0 and shape["threads"] in (256, 512) and shape["cluster"] in (1, 2, 4, 8)
+    u, st = bt.solve(1.0, nus, fx, fv, plane="strain", precision="mixed", precond="block_jacobi",
+                     rtol=1e-10)
+    for p, up, s in zip(probs, bt.split(u), st):
+        assert s["status"] == 0 and s["ms"] > 0
+        assert _rel(up, _single(sfem, ctx, p)) <= TOL_U
+    bt.close()
