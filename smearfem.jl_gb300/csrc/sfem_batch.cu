@@ -27,19 +27,7 @@
 #include <type_traits>
 #include <vector>
 
-#include <cooperative_groups.h>
-
-#include "sfem_internal.cuh"
-
-namespace cgrp = cooperative_groups;
-
-struct BatchMesh {
-    int64_t node0, nnode;      // combined (padded) node range start, real node count
-    int64_t slice0, slice1;    // its slices
-    int64_t elem0, elem1;      // its elements in the combined numbering
-    int64_t dof0, ndof;        // its block of u: global DOFs [dof0, dof0 + ndof)
-    int64_t fix0, fix1;        // its entries of the fixed-DOF arrays
-};
+#include "sfem_meshsolve.cuh"
 
 struct sfem_batch {
     sfem_ctx *ctx = nullptr;
@@ -68,690 +56,8 @@ struct sfem_batch {
 
 namespace {
 
-struct ElemTableB {
-    double dN[8][9][3];
-    double w[8];
-    unsigned char pa[48], pb[48];
-};
+using namespace sfem_dev;
 
-ElemTableB make_table_b(int ndim, int fclass) {
-    ElemTableB t;
-    memset(&t, 0, sizeof(t));
-    double xi[2], w[2];
-    sfem_gaussian_quadrature(-1, 1, 2, xi, w);
-    const int ox[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, oz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
-    const int ngp = ndim == 2 ? 4 : 8;
-    const int nen = fclass == SFEM_Q2 ? 9 : (1 << ndim);
-    for (int g = 0; g < ngp; ++g) {
-        double N[9], dN[27];
-        if (ndim == 2) {
-            t.w[g] = w[ox[g]] * w[oy[g]];
-            sfem_basis_function(2, fclass, xi[ox[g]], xi[oy[g]], 0.0, N, dN);
-        } else {
-            t.w[g] = w[ox[g]] * w[oy[g]] * w[oz[g]];
-            sfem_basis_function(3, fclass, xi[ox[g]], xi[oy[g]], xi[oz[g]], N, dN);
-        }
-        for (int a = 0; a < nen; ++a)
-            for (int k = 0; k < ndim; ++k) t.dN[g][a][k] = dN[k * nen + a];
-    }
-    int p = 0;
-    for (int a = 0; a < nen; ++a)
-        for (int b = a; b < nen; ++b) {
-            t.pa[p] = (unsigned char)a;
-            t.pb[p] = (unsigned char)b;
-            ++p;
-        }
-    return t;
-}
-
-struct BatchArgs {
-    const BatchMesh *meshes;
-    const int *order;     // large meshes first (cluster work), then small ones
-    int64_t nmesh, nbig;  // meshes in `order`, of which the first nbig are large
-    int64_t nmesh_all;    // meshes in the batch (per-mesh material arrays)
-    unsigned *queue;      // [0]: next large mesh, [1]: next small mesh
-    // combined mesh
-    const double *X;
-    const int *ien;
-    int64_t nEl;
-    const int64_t *n2e_ptr;
-    const int *n2e;
-    const int *rowlen;
-    const int64_t *sliceptr;
-    const int *col;
-    const int *g2i;
-    const int *id;   // [b][nN] combined global DOF (0-based) of (node, comp); null for b == 1
-    int64_t nN, n_global;
-    // material and boundary data
-    const double *E;
-    int64_t nE;      // 1, nmesh or nEl (combined)
-    const double *nu;
-    int64_t nNu;
-    int plane;
-    const int64_t *fix_dofs;  // mesh-local, 1-based
-    const double *fix_vals;
-    // buffers
-    double *kbuf, *val64;
-    float *val32;
-    unsigned char *fixed, *gfixed;
-    double *ud, *b64, *x64, *q64;
-    void *vecT;      // x, r, z, p, q (type T, nd each) then minv (nN * b * b)
-    int64_t nd;
-    double *u_out;
-    // solver
-    double rtol, delta2;
-    int maxit, block_jacobi;
-    sfem_batch_stats *stats;
-    DevErr *err;
-};
-
-// Internal index (node*B + comp) of the mesh-local DOF gl (0-based), or -1
-// when no element uses it.  Scalar meshes have no ID: DOF = node.
-template <int B>
-__device__ __forceinline__ int local_to_internal(const BatchArgs &a, const BatchMesh &M, int64_t gl) {
-    const int64_t g = B == 1 ? M.node0 + gl : M.dof0 + gl;
-    return g < a.n_global ? a.g2i[g] : -1;
-}
-
-// Output position (global DOF of u) of internal DOF (node, comp).
-template <int B>
-__device__ __forceinline__ int64_t internal_to_output(const BatchArgs &a, const BatchMesh &M, int64_t node, int comp) {
-    return B == 1 ? M.dof0 + (node - M.node0) : (int64_t)a.id[(int64_t)comp * a.nN + node];
-}
-
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// CTA-wide sums of (a, b) in a fixed order, returned to every thread.
-__device__ double2 block_sum2(double a, double b, double *sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    a = warp_sum_d(a);
-    b = warp_sum_d(b);
-    if (lane == 0) {
-        sh[warp] = a;
-        sh[32 + warp] = b;
-    }
-    __syncthreads();
-    double x = 0.0, y = 0.0;
-    for (int w = 0; w < nw; ++w) {
-        x += sh[w];
-        y += sh[32 + w];
-    }
-    __syncthreads();
-    return make_double2(x, y);
-}
-
-// y = (mask ? 0 : K x) over the mesh's slices; returns this thread's x.y share.
-// Rows at or beyond `rend` (the padding that rounds a mesh up to whole
-// slices) are neither written nor counted: their vector entries are unset.
-// Slices sfirst, sfirst + sstride, ... below s1 (one warp each).
-template <typename T, int B>
-__device__ double grp_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val,
-                           int64_t sfirst, int64_t s1, int64_t sstride, int64_t rend, const T *__restrict__ x,
-                           T *__restrict__ y, const unsigned char *__restrict__ fixed, bool masked) {
-    const int lane = threadIdx.x & 31;
-    double dot = 0.0;
-    for (int64_t s = sfirst; s < s1; s += sstride) {
-        const int64_t r = s * 32 + lane;
-        const int64_t k0 = sliceptr[s], k1 = sliceptr[s + 1];
-        T acc[B];
-#pragma unroll
-        for (int i = 0; i < B; ++i) acc[i] = T(0);
-#pragma unroll 2
-        for (int64_t k = k0; k < k1; ++k) {
-            const int c = col[k * 32 + lane];
-            T v[B * B];
-#pragma unroll
-            for (int e = 0; e < B * B; ++e) v[e] = val[(k * B * B + e) * 32 + lane];
-#pragma unroll
-            for (int i = 0; i < B; ++i)
-#pragma unroll
-                for (int j = 0; j < B; ++j) acc[i] = fma(v[i * B + j], x[(int64_t)c * B + j], acc[i]);
-        }
-        if (r < rend) {
-#pragma unroll
-            for (int i = 0; i < B; ++i) {
-                const int64_t d = r * B + i;
-                const T out = (masked && fixed[d]) ? T(0) : acc[i];
-                y[d] = out;
-                dot += (double)x[d] * (double)out;
-            }
-        }
-    }
-    return dot;
-}
-
-// One CTA working alone on a mesh.
-struct SoloGroup {
-    __device__ __forceinline__ int rank() const { return 0; }
-    __device__ __forceinline__ int size() const { return 1; }
-    __device__ __forceinline__ void sync() const { __syncthreads(); }
-    __device__ double2 sum2(double a, double b, double *red, double *) const { return block_sum2(a, b, red); }
-    __device__ int max_flag(int *flag) const {
-        __syncthreads();
-        const int f = *flag;
-        __syncthreads();
-        return f;
-    }
-};
-
-// A thread-block cluster working together on a mesh: hardware cluster
-// barrier, partial sums exchanged through distributed shared memory and
-// added in rank order (deterministic).
-struct ClusterGroup {
-    __device__ __forceinline__ int rank() const { return (int)cgrp::this_cluster().block_rank(); }
-    __device__ __forceinline__ int size() const { return (int)cgrp::this_cluster().num_blocks(); }
-    __device__ __forceinline__ void sync() const { cgrp::this_cluster().sync(); }
-    __device__ double2 sum2(double a, double b, double *red, double *xch) const {
-        const double2 p = block_sum2(a, b, red);
-        cgrp::cluster_group cl = cgrp::this_cluster();
-        if (threadIdx.x == 0) {
-            xch[0] = p.x;
-            xch[1] = p.y;
-        }
-        cl.sync();
-        double x = 0.0, y = 0.0;
-        for (unsigned r = 0; r < cl.num_blocks(); ++r) {
-            const double *rx = cl.map_shared_rank(xch, r);
-            x += rx[0];
-            y += rx[1];
-        }
-        cl.sync();
-        return make_double2(x, y);
-    }
-    __device__ int max_flag(int *flag) const {
-        cgrp::cluster_group cl = cgrp::this_cluster();
-        cl.sync();
-        int f = 0;
-        for (unsigned r = 0; r < cl.num_blocks(); ++r) f = max(f, *cl.map_shared_rank(flag, r));
-        cl.sync();
-        return f;
-    }
-};
-
-// Assemble and solve mesh `mb` with group G (a CTA or a cluster).
-template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED>
-__device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
-                             int *s_flag) {
-    using T = typename std::conditional<MIXED, float, double>::type;
-    constexpr int GS = NEN * NDIM + 1;
-    constexpr int NPAIR = NEN * (NEN + 1) / 2;
-    extern __shared__ double smem[];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const int grank = G.rank(), gsize = G.size();
-    const int64_t gt = (int64_t)grank * blockDim.x + tid, gstride = (int64_t)gsize * blockDim.x;
-    const int64_t gw = (int64_t)grank * nw + warp, gnw = (int64_t)gsize * nw;
-    const int ngroups = nw / NGP;  // element groups of NGP warps
-    const int grp = warp / NGP, gp = warp % NGP;
-    double *sG = smem + (int64_t)grp * (NGP * 32 * GS + NGP * 32);
-    double *sW = sG + NGP * 32 * GS;
-    T *xv = (T *)a.vecT;
-    T *rv = xv + a.nd, *zv = rv + a.nd, *pv = zv + a.nd, *qv = pv + a.nd;
-    T *minv = qv + a.nd;  // [nN][B][B]
-    const T *valT = MIXED ? (const T *)a.val32 : (const T *)a.val64;
-    const BatchMesh M = a.meshes[mb];
-    unsigned long long t_start = 0;
-    if (tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
-    {
-        const int64_t n0 = M.node0, n1 = M.node0 + M.nnode;      // real nodes
-        const int64_t d0 = n0 * B, d1 = (M.node0 + ((M.nnode + 31) / 32) * 32) * B;  // padded DOF range
-
-        // ---- 1. element stiffness (FP64), NGP warps per group of 32 elements
-        const int64_t nel = M.elem1 - M.elem0;
-        const int64_t rounds = (nel + 32 * ngroups * gsize - 1) / (32 * ngroups * gsize);
-        for (int64_t rd = 0; rd < rounds; ++rd) {
-            const int64_t e = M.elem0 + ((rd * gsize + grank) * ngroups + grp) * 32 + lane;
-            const bool live = grp < ngroups && e < M.elem1;
-            if (live) {
-                double xe[NEN][NDIM];
-#pragma unroll
-                for (int an = 0; an < NEN; ++an) {
-                    const int node = a.ien[(int64_t)an * a.nEl + e];
-#pragma unroll
-                    for (int i = 0; i < NDIM; ++i) xe[an][i] = a.X[(int64_t)node * NDIM + i];
-                }
-                double J[NDIM][NDIM];
-#pragma unroll
-                for (int i = 0; i < NDIM; ++i)
-#pragma unroll
-                    for (int k = 0; k < NDIM; ++k) {
-                        double s = 0.0;
-#pragma unroll
-                        for (int an = 0; an < NEN; ++an) s = fma(xe[an][i], tab.dN[gp][an][k], s);
-                        J[i][k] = s;
-                    }
-                double det, inv[NDIM][NDIM];
-                if (NDIM == 2) {
-                    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-                    const double r = 1.0 / det;
-                    inv[0][0] = J[1][1] * r;
-                    inv[0][1] = -J[0][1] * r;
-                    inv[1][0] = -J[1][0] * r;
-                    inv[1][1] = J[0][0] * r;
-                } else {
-                    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-                    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-                    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-                    det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-                    const double r = 1.0 / det;
-                    inv[0][0] = c00 * r;
-                    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
-                    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
-                    inv[1][0] = c01 * r;
-                    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
-                    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
-                    inv[2][0] = c02 * r;
-                    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
-                    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
-                }
-                if (det == 0.0) sfem_dev_error(a.err, SFEM_SINGULAR_JACOBIAN, e);
-                double *g = sG + ((int64_t)gp * 32 + lane) * GS;
-#pragma unroll
-                for (int an = 0; an < NEN; ++an)
-#pragma unroll
-                    for (int k = 0; k < NDIM; ++k) {
-                        double s = 0.0;
-#pragma unroll
-                        for (int j = 0; j < NDIM; ++j) s = fma(tab.dN[gp][an][j], inv[j][k], s);
-                        g[an * NDIM + k] = s;
-                    }
-                sW[gp * 32 + lane] = tab.w[gp] * fabs(det);
-            }
-            __syncthreads();
-            if (live) {
-                double lam = 0.0, mu = 0.0;
-                if (B > 1) {
-                    const int64_t iE = a.nE == 1 ? 0 : (a.nE == a.nmesh_all ? mb : e);
-                    const int64_t iN = a.nNu == 1 ? 0 : (a.nNu == a.nmesh_all ? mb : e);
-                    const double E = a.E[iE], nu = a.nu[iN];
-                    if (NDIM == 2 && a.plane == SFEM_PLANE_STRESS) {
-                        lam = nu * E / (1 - nu * nu);
-                        mu = E / (2 * (1 + nu));
-                    } else {
-                        const double c = E / ((1 + nu) * (1 - 2 * nu));
-                        lam = nu * c;
-                        mu = (1 - 2 * nu) / 2 * c;
-                    }
-                }
-                for (int p = gp; p < NPAIR; p += NGP) {
-                    const int pa = tab.pa[p], pb = tab.pb[p];
-                    if (B == 1) {
-                        double s = 0.0;
-#pragma unroll
-                        for (int qg = 0; qg < NGP; ++qg) {
-                            const double *g = sG + ((int64_t)qg * 32 + lane) * GS;
-                            double dd = 0.0;
-#pragma unroll
-                            for (int k = 0; k < NDIM; ++k) dd = fma(g[pa * NDIM + k], g[pb * NDIM + k], dd);
-                            s = fma(sW[qg * 32 + lane], dd, s);
-                        }
-                        a.kbuf[(int64_t)p * a.nEl + e] = s;
-                    } else {
-                        double S[NDIM][NDIM];
-#pragma unroll
-                        for (int i = 0; i < NDIM; ++i)
-#pragma unroll
-                            for (int j = 0; j < NDIM; ++j) S[i][j] = 0.0;
-#pragma unroll
-                        for (int qg = 0; qg < NGP; ++qg) {
-                            const double *g = sG + ((int64_t)qg * 32 + lane) * GS;
-                            const double wq = sW[qg * 32 + lane];
-#pragma unroll
-                            for (int i = 0; i < NDIM; ++i) {
-                                const double wa = wq * g[pa * NDIM + i];
-#pragma unroll
-                                for (int j = 0; j < NDIM; ++j) S[i][j] = fma(wa, g[pb * NDIM + j], S[i][j]);
-                            }
-                        }
-                        if (pa == pb) {
-#pragma unroll
-                            for (int i = 0; i < NDIM; ++i)
-#pragma unroll
-                                for (int j = 0; j < i; ++j) S[i][j] = S[j][i];
-                        }
-                        double tr = 0.0;
-#pragma unroll
-                        for (int i = 0; i < NDIM; ++i) tr += S[i][i];
-#pragma unroll
-                        for (int i = 0; i < NDIM; ++i)
-#pragma unroll
-                            for (int j = 0; j < NDIM; ++j) {
-                                double v = lam * S[i][j] + mu * S[j][i];
-                                if (i == j) v += mu * tr;
-                                a.kbuf[((int64_t)p * B * B + i * B + j) * a.nEl + e] = v;
-                            }
-                    }
-                }
-            }
-            __syncthreads();
-        }
-
-        G.sync();  // every element block of the mesh is in kbuf
-        // ---- 2. gather into the mesh's K blocks (ascending element order)
-        for (int64_t s = M.slice0 + gw; s < M.slice1; s += gnw) {
-            const int64_t r64 = s * 32 + lane;
-            const int r = (int)r64;
-            const bool liver = r64 < a.nN;
-            const int64_t slab0 = a.sliceptr[s], width = a.sliceptr[s + 1] - slab0;
-            const int len = liver ? a.rowlen[r] : 0;
-            const int64_t q0 = liver ? a.n2e_ptr[r] : 0, q1 = liver ? a.n2e_ptr[r + 1] : 0;
-            for (int64_t k = 0; k < width; ++k) {
-                const int64_t slab = slab0 + k;
-                double acc[B * B];
-#pragma unroll
-                for (int i = 0; i < B * B; ++i) acc[i] = 0.0;
-                if (k < len) {
-                    const int c = a.col[slab * 32 + lane];
-                    int prev = -1;
-                    for (int64_t qq = q0; qq < q1; ++qq) {
-                        const int e = a.n2e[qq];
-                        if (e == prev) continue;
-                        prev = e;
-                        int nodes[NEN];
-#pragma unroll
-                        for (int an = 0; an < NEN; ++an) nodes[an] = a.ien[(int64_t)an * a.nEl + e];
-#pragma unroll
-                        for (int an = 0; an < NEN; ++an) {
-                            if (nodes[an] != r) continue;
-#pragma unroll
-                            for (int bq = 0; bq < NEN; ++bq) {
-                                if (nodes[bq] != c) continue;
-                                if (an <= bq) {
-                                    const int64_t base = (int64_t)sfem_pair(an, bq, NEN) * B * B;
-#pragma unroll
-                                    for (int i = 0; i < B * B; ++i) acc[i] += a.kbuf[(base + i) * a.nEl + e];
-                                } else {
-                                    const int64_t base = (int64_t)sfem_pair(bq, an, NEN) * B * B;
-#pragma unroll
-                                    for (int i = 0; i < B; ++i)
-#pragma unroll
-                                        for (int j = 0; j < B; ++j)
-                                            acc[i * B + j] += a.kbuf[(base + j * B + i) * a.nEl + e];
-                                }
-                            }
-                        }
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < B * B; ++i) {
-                    a.val64[(slab * B * B + i) * 32 + lane] = acc[i];
-                    if (MIXED) a.val32[(slab * B * B + i) * 32 + lane] = (float)acc[i];
-                }
-            }
-        }
-        if (tid == 0) *s_flag = SFEM_OK;
-        G.sync();
-
-        // ---- 3. Dirichlet set-up
-        for (int64_t d = d0 + gt; d < d1; d += gstride) {
-            const int64_t node = d / B;
-            a.fixed[d] = (node >= n1 || a.rowlen[node] == 0) ? 1 : 0;
-            a.ud[d] = 0.0;
-            a.x64[d] = 0.0;
-            xv[d] = T(0);
-        }
-        for (int64_t g = M.dof0 + gt; g < M.dof0 + M.ndof; g += gstride) a.gfixed[g] = 0;
-        G.sync();
-        for (int64_t t = M.fix0 + gt; t < M.fix1; t += gstride) {
-            const int64_t gl = a.fix_dofs[t] - 1;
-            if (gl < 0 || gl >= M.ndof) {
-                atomicMax(s_flag, (int)SFEM_BAD_INDEX);
-                continue;
-            }
-            a.gfixed[M.dof0 + gl] = 1;
-            const int i = local_to_internal<B>(a, M, gl);
-            if (i >= 0) {
-                a.fixed[i] = 1;
-                a.ud[i] = a.fix_vals[t];
-            }
-        }
-        G.sync();
-        for (int64_t gl = gt; gl < M.ndof; gl += gstride) {
-            if (local_to_internal<B>(a, M, gl) < 0 && !a.gfixed[M.dof0 + gl])
-                atomicMax(s_flag, (int)SFEM_SINGULAR);  // a free DOF with no row in K
-        }
-        // b = -K q_d on the free DOFs (FP64)
-        grp_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.ud, a.q64, a.fixed, false);
-        G.sync();
-        for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) a.b64[d] = a.fixed[d] ? 0.0 : -a.q64[d];
-
-        // ---- 4. preconditioner: inverse of each node's free-restricted diagonal block
-        for (int64_t node = n0 + gt; node < n1; node += gstride) {
-            double D[B][B];
-#pragma unroll
-            for (int i = 0; i < B; ++i)
-#pragma unroll
-                for (int j = 0; j < B; ++j) D[i][j] = 0.0;
-            const int len = a.rowlen[node];
-            const int64_t slab0 = a.sliceptr[node >> 5];
-            const int ln = (int)(node & 31);
-            for (int k = 0; k < len; ++k)
-                if (a.col[(slab0 + k) * 32 + ln] == (int)node) {
-#pragma unroll
-                    for (int i = 0; i < B; ++i)
-#pragma unroll
-                        for (int j = 0; j < B; ++j) D[i][j] = a.val64[((slab0 + k) * B * B + i * B + j) * 32 + ln];
-                    break;
-                }
-            bool fx[B];
-#pragma unroll
-            for (int i = 0; i < B; ++i) fx[i] = a.fixed[node * B + i] != 0;
-            double I[B][B];
-            bool bad = false;
-            if (B == 1 || !a.block_jacobi) {
-#pragma unroll
-                for (int i = 0; i < B; ++i)
-#pragma unroll
-                    for (int j = 0; j < B; ++j) I[i][j] = 0.0;
-#pragma unroll
-                for (int i = 0; i < B; ++i)
-                    if (!fx[i]) {
-                        if (!(D[i][i] != 0.0)) bad = true;
-                        else I[i][i] = 1.0 / D[i][i];
-                    }
-            } else {
-#pragma unroll
-                for (int i = 0; i < B; ++i)
-#pragma unroll
-                    for (int j = 0; j < B; ++j)
-                        if (fx[i] || fx[j]) D[i][j] = (i == j) ? 1.0 : 0.0;
-                double det;
-                if (B == 2) {
-                    det = D[0][0] * D[1][1] - D[0][1] * D[1][0];
-                    I[0][0] = D[1][1];
-                    I[0][1] = -D[0][1];
-                    I[1][0] = -D[1][0];
-                    I[1][1] = D[0][0];
-                } else {
-                    I[0][0] = D[1][1] * D[2][2] - D[1][2] * D[2][1];
-                    I[0][1] = D[0][2] * D[2][1] - D[0][1] * D[2][2];
-                    I[0][2] = D[0][1] * D[1][2] - D[0][2] * D[1][1];
-                    I[1][0] = D[1][2] * D[2][0] - D[1][0] * D[2][2];
-                    I[1][1] = D[0][0] * D[2][2] - D[0][2] * D[2][0];
-                    I[1][2] = D[0][2] * D[1][0] - D[0][0] * D[1][2];
-                    I[2][0] = D[1][0] * D[2][1] - D[1][1] * D[2][0];
-                    I[2][1] = D[0][1] * D[2][0] - D[0][0] * D[2][1];
-                    I[2][2] = D[0][0] * D[1][1] - D[0][1] * D[1][0];
-                    det = D[0][0] * I[0][0] + D[0][1] * I[1][0] + D[0][2] * I[2][0];
-                }
-                if (!(det != 0.0)) bad = true;
-                const double rd = det != 0.0 ? 1.0 / det : 0.0;
-#pragma unroll
-                for (int i = 0; i < B; ++i)
-#pragma unroll
-                    for (int j = 0; j < B; ++j) I[i][j] = (fx[i] || fx[j]) ? 0.0 : I[i][j] * rd;
-            }
-            if (bad) atomicMax(s_flag, (int)SFEM_SINGULAR);
-#pragma unroll
-            for (int i = 0; i < B; ++i)
-#pragma unroll
-                for (int j = 0; j < B; ++j) minv[(node * B + i) * B + j] = (T)I[i][j];
-        }
-        G.sync();
-
-        // ---- 5. preconditioned CG
-        double rz = 0.0, bb = 0.0;
-        {
-            double prz = 0.0, pbb = 0.0;
-            for (int64_t node = n0 + gt; node < n1; node += gstride) {
-                T r[B];
-#pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    const double bv = a.b64[node * B + i];
-                    r[i] = (T)bv;
-                    rv[node * B + i] = r[i];
-                    pv[node * B + i] = T(0);
-                    pbb += bv * bv;
-                }
-#pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    T zi = T(0);
-#pragma unroll
-                    for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
-                    zv[node * B + i] = zi;
-                    prz += (double)(r[i] * zi);
-                }
-            }
-            const double2 t = G.sum2(prz, pbb, red, xch);
-            rz = t.x;
-            bb = t.y;
-        }
-        const double tol2 = a.rtol * a.rtol * bb;
-        double rr_ref = bb, rr = bb, beta = 0.0;
-        int it = 0, refreshes = 0, status = G.max_flag(s_flag);
-        bool done = status != SFEM_OK || !(bb > 0.0);
-        while (!done) {
-            // p = z + beta p
-            for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) pv[d] = fma((T)beta, pv[d], zv[d]);
-            G.sync();
-            double pq = grp_spmv<T, B>(a.sliceptr, a.col, valT, M.slice0 + gw, M.slice1, gnw, n1, pv, qv, a.fixed, true);
-            pq = G.sum2(pq, 0.0, red, xch).x;
-            if (!(pq > 0.0)) {
-                status = SFEM_SINGULAR;
-                break;
-            }
-            const T alpha = (T)(rz / pq);
-            double prz = 0.0, prr = 0.0;
-            for (int64_t node = n0 + gt; node < n1; node += gstride) {
-                T r[B];
-#pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    const int64_t d = node * B + i;
-                    xv[d] = fma(alpha, pv[d], xv[d]);
-                    r[i] = fma(-alpha, qv[d], rv[d]);
-                    rv[d] = r[i];
-                    prr += (double)(r[i] * r[i]);
-                }
-#pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    T zi = T(0);
-#pragma unroll
-                    for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
-                    zv[node * B + i] = zi;
-                    prz += (double)(r[i] * zi);
-                }
-            }
-            const double2 t = G.sum2(prz, prr, red, xch);
-            ++it;
-            const double rz_prev = rz;
-            rz = t.x;
-            rr = t.y;
-            beta = rz_prev != 0.0 ? rz / rz_prev : 0.0;
-            if (!(rr == rr)) {
-                status = SFEM_SINGULAR;
-                break;
-            }
-            const bool at_tol = rr <= tol2, at_max = it >= a.maxit;
-            if (!MIXED) {
-                if (at_tol) break;
-                if (at_max) {
-                    status = SFEM_NOT_CONVERGED;
-                    break;
-                }
-                continue;
-            }
-            if (at_tol || at_max || rr <= a.delta2 * rr_ref) {
-                // FP64 refresh: fold the FP32 iterate, recompute r = b - K x in FP64
-                for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) {
-                    a.x64[d] += (double)xv[d];
-                    xv[d] = T(0);
-                }
-                G.sync();
-                grp_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.x64, a.q64,
-                                    a.fixed, true);
-                G.sync();
-                double frz = 0.0, frr = 0.0;
-                for (int64_t node = n0 + gt; node < n1; node += gstride) {
-                    T r[B];
-#pragma unroll
-                    for (int i = 0; i < B; ++i) {
-                        const int64_t d = node * B + i;
-                        const double v = a.fixed[d] ? 0.0 : a.b64[d] - a.q64[d];
-                        r[i] = (T)v;
-                        rv[d] = r[i];
-                        frr += v * v;
-                    }
-#pragma unroll
-                    for (int i = 0; i < B; ++i) {
-                        T zi = T(0);
-#pragma unroll
-                        for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
-                        zv[node * B + i] = zi;
-                        frz += (double)(r[i] * zi);
-                    }
-                }
-                const double2 f = G.sum2(frz, frr, red, xch);
-                ++refreshes;
-                rz = f.x;
-                rr = f.y;
-                rr_ref = rr;
-                beta = rz_prev != 0.0 ? rz / rz_prev : 0.0;
-                if (rr <= tol2) break;
-                if (at_max) {
-                    status = SFEM_NOT_CONVERGED;
-                    break;
-                }
-            }
-        }
-        if (!MIXED && status != SFEM_SINGULAR) {
-            for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) a.x64[d] = (double)xv[d];
-        }
-        G.sync();
-
-        // ---- 6. u = q_d + x in the mesh's DOF numbering
-        for (int64_t node = n0 + gt; node < n1; node += gstride) {
-            if (a.rowlen[node] == 0) continue;
-#pragma unroll
-            for (int i = 0; i < B; ++i) {
-                const int64_t g = internal_to_output<B>(a, M, node, i);
-                if (g >= 0) a.u_out[g] = a.ud[node * B + i] + a.x64[node * B + i];
-            }
-        }
-        for (int64_t t = M.fix0 + gt; t < M.fix1; t += gstride) {  // prescribed DOFs outside K
-            const int64_t gl = a.fix_dofs[t] - 1;
-            if (gl < 0 || gl >= M.ndof) continue;
-            if (local_to_internal<B>(a, M, gl) < 0) a.u_out[M.dof0 + gl] = a.fix_vals[t];
-        }
-        if (grank == 0 && tid == 0) {
-            unsigned long long t_end;
-            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
-            sfem_batch_stats st;
-            st.status = status;
-            st.iterations = it;
-            st.refreshes = refreshes;
-            st.group_ctas = gsize;
-            st.relres = bb > 0.0 ? sqrt(rr / bb) : 0.0;
-            st.ms = (double)(t_end - t_start) * 1e-6;
-            a.stats[mb] = st;
-        }
-    }
-}
-
-// 2D classes fit two 512-thread CTAs per SM (64 registers); 3D elasticity
-// needs the full register file of one.
 template <int NDIM, int NEN, int NGP, int B, bool MIXED>
 __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
     __shared__ double red[64];
