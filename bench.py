@@ -55,11 +55,14 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ne", type=int, default=128)
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--legs", default="value,mixed,e2e,cpu,batch",
-                    help="comma list of value,mixed,e2e,cpu,batch (profiling runs pick one)")
+    ap.add_argument("--legs", default="value,mixed,e2e,cpu,batch,serve",
+                    help="comma list of value,mixed,e2e,cpu,batch,serve (profiling runs pick one)")
     ap.add_argument("--batch-count", type=int, default=1024, help="meshes in the batch leg")
     ap.add_argument("--batch-rtol", type=float, default=1e-12,
                     help="batch-leg relative residual (1e-12 keeps the error in u under 1e-8)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
+    ap.add_argument("--serve-requests", type=int, default=240, help="requests in the saturating stream")
+    ap.add_argument("--serve-pool", type=int, default=96, help="distinct meshes the stream draws from")
     ap.add_argument("--no-extras", action="store_true", help="same as --legs value")
     a = ap.parse_args(argv)
     a.legs = {"value"} if a.no_extras else set(x.strip() for x in a.legs.split(",") if x.strip())
@@ -421,6 +424,8 @@ def our_arm(args, dist):
                        "rel_err": float(np.linalg.norm(hU - uref_h) / np.linalg.norm(uref_h))}
     if "batch" in args.legs:
         line["batch"] = batch_leg(args, pkg, ctx, stream, dist)
+    if "serve" in args.legs:
+        line["serve"] = serve_leg(args, pkg, ctx, dist)
     if "cpu" in args.legs and dist.world == 1:
         # ---- CPU baseline (rank 0, N=1 only)
         v, det = cpu_sample(pkg, args.ne, n_dof, nnz, it)
@@ -506,6 +511,115 @@ def batch_leg(args, pkg, ctx, stream, dist):
             "plain_fp64_gpu": {"value": n_total / t_plain, "s": t_plain,
                                "path": "single-mesh API per mesh: assemble + FP64 Jacobi-PCG"},
             "speedup_vs_plain_fp64": (n_total / (ms * 1e-3)) / (n_total / t_plain)}
+
+
+def _stream(servers, pool, arrivals, which):
+    """Open-loop driver: a thread submits pool[which[i]] at arrivals[i] (s);
+    the caller's thread collects results.  Returns per-request records and
+    the wall time from the first submission to the last result."""
+    import threading
+    n = len(arrivals)
+    ids = [None] * n
+    ready = [threading.Event() for _ in range(n)]
+    t0 = time.perf_counter()
+
+    def submitter():
+        for i in range(n):
+            d = t0 + arrivals[i] - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            p = pool[which[i]]
+            srv = servers[p.ndim]
+            ids[i] = (srv, srv.submit(p.NodeList, p.IEN[: p.n_elem], p.ID, p.Young, p.nu,
+                                      p.fixed_dofs, p.fixed_vals, topology_key=p.ne))
+            ready[i].set()
+
+    th = threading.Thread(target=submitter, daemon=True)
+    th.start()
+    recs, t_last = [], t0
+    for i in range(n):
+        ready[i].wait()
+        srv, rid = ids[i]
+        u, res = srv.wait(rid)
+        t_last = max(t_last, time.perf_counter())
+        recs.append((which[i], u, res))
+    th.join()
+    return recs, t_last - t0
+
+
+def serve_leg(args, pkg, ctx, dist):
+    """Serving workload: an open-loop Poisson stream, 70% plane-strain quads
+    n ~ U{32..512}, 30% hexes n ~ U{16..64}, per-element E ~ lognormal(0, 0.5),
+    nu ~ U(0.25, 0.45) per request, seeded boundary displacements; one server
+    per element class (2D: 55% of the GPU's CTA slots, 3D: 35%), topology key
+    = mesh size, mixed-precision block-Jacobi PCG.  Requests draw from a pool
+    of distinct meshes, so a repeated request must give the same bits."""
+    rng = np.random.default_rng(2005)
+    pool = [p for _, p in pkg.meshgen.config5_stream(args.serve_pool)]
+    rtol = args.batch_rtol
+    kw = dict(precision="mixed", precond="block_jacobi", rtol=rtol, cluster=4, idle_exit_ms=200.0)
+    servers = {2: pkg.Server(ndim=2, nDof=2, plane="strain", sm_fraction=0.55, **kw),
+               3: pkg.Server(ndim=3, nDof=3, sm_fraction=0.35, **kw)}
+    try:
+        # warm-up: every pool mesh once (builds and caches each topology's pattern)
+        recs, t_warm = _stream(servers, pool, np.zeros(len(pool)), np.arange(len(pool)))
+        first = {k: u for k, u, _ in recs}
+        # saturation: the offered rate far above capacity
+        n = args.serve_requests
+        arr = np.cumsum(rng.exponential(1.0 / args.serve_rate, n))
+        which = rng.integers(0, len(pool), n)
+        recs, wall = _stream(servers, pool, arr, which)
+        lat = np.array([r["total_ms"] for _, _, r in recs])
+        gpu = np.array([r["gpu_ms"] for _, _, r in recs])
+        dofs = float(sum(r["ndof"] for _, _, r in recs))
+        same = sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs)
+        capacity = n / wall
+        peak = {d: servers[d].info() for d in servers}
+        # below capacity: latency without a backlog
+        m = max(20, min(120, int(capacity * 8)))
+        rate = 0.5 * capacity
+        arr2 = np.cumsum(rng.exponential(1.0 / rate, m))
+        which2 = rng.integers(0, len(pool), m)
+        recs2, wall2 = _stream(servers, pool, arr2, which2)
+        lat2 = np.array([r["total_ms"] for _, _, r in recs2])
+        same += sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs2)
+        statuses_ok = sum(r["status"] == 0 for _, _, r in recs + recs2)
+        info = {d: servers[d].info() for d in servers}
+    finally:
+        for s_ in servers.values():
+            s_.close()
+    # error against tight FP64 solves, and the plain FP64 GPU path, on a sample of the pool
+    sample = list(range(0, len(pool), max(1, len(pool) // 16)))
+    errs, t_plain, dof_plain = [], 0.0, 0
+    for k in sample:
+        p = pool[k]
+        K = pkg.assemble_system(p.ne, p.NodeList, p.IEN, p.ndim, "Q1", p.ndim, p.ID, p.Young,
+                                float(p.nu[0]), plane=p.plane, ctx=ctx, as_handle=True)
+        t0 = time.perf_counter()
+        K.solve(p.fixed_dofs, p.fixed_vals, rtol=rtol)
+        t_plain += time.perf_counter() - t0
+        ref = K.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13)[0]
+        K.close()
+        dof_plain += p.n_dof
+        errs.append(float(np.linalg.norm(first[k] - ref) / np.linalg.norm(ref)))
+    pct = lambda a, q: float(np.percentile(a, q))  # noqa: E731
+    return {"workload": f"open-loop Poisson stream at {args.serve_rate:g} req/s, {n} requests "
+                        f"from a pool of {len(pool)} meshes (70% quads n~U{{32..512}}, 30% hexes "
+                        f"n~U{{16..64}}), mixed block-Jacobi PCG to {rtol:g}",
+            "solves_per_s": capacity, "dof_per_s": dofs / wall, "unit": "requests/s",
+            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max())},
+            "gpu_ms": {"p50": pct(gpu, 50), "p99": pct(gpu, 99)},
+            "below_capacity": {"rate": rate, "requests": m, "solves_per_s": m / wall2,
+                               "latency_ms": {"p50": pct(lat2, 50), "p99": pct(lat2, 99)}},
+            "repeat_bitwise_identical": f"{same}/{n + m}", "statuses_ok": int(statuses_ok),
+            "warmup_s": t_warm, "peak_inflight": {d: peak[d]["peak_inflight"] for d in peak},
+            "peak_bytes": {d: info[d]["peak_bytes"] for d in info},
+            "kernel_launches": {d: info[d]["kernel_launches"] for d in info},
+            "grid": {d: [info[d]["grid"], info[d]["cluster"]] for d in info},
+            "rel_err_max_sample": max(errs),
+            "plain_fp64_gpu": {"dof_per_s": dof_plain / t_plain,
+                               "path": "single-mesh API per request: FP64 Jacobi-PCG (solve only)"},
+            "speedup_vs_plain_fp64": (dofs / wall) / (dof_plain / t_plain)}
 
 
 def main(argv=None):

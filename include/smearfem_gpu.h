@@ -56,7 +56,8 @@ typedef enum {
     SFEM_NOT_CONVERGED = 5,      /* maxit reached before rtol                         */
     SFEM_CUDA_ERROR = 6,         /* CUDA runtime error                                */
     SFEM_SINGULAR = 7,           /* K_free singular: zero pivot / CG breakdown        */
-    SFEM_UNSUPPORTED = 8         /* element class the reference cannot assemble       */
+    SFEM_UNSUPPORTED = 8,        /* element class the reference cannot assemble       */
+    SFEM_TIMEOUT = 9             /* a wait ended before the request finished          */
 } sfem_status;
 
 enum { SFEM_MEM_HOST = 0, SFEM_MEM_DEVICE = 1 };
@@ -292,6 +293,66 @@ SFEM_API int sfem_batch_autotune(sfem_ctx *ctx, sfem_batch *batch, int plane, co
 SFEM_API int sfem_batch_get_launch(const sfem_batch *batch, int *threads, int *ctas_per_sm,
                                    int *cluster, int64_t *cluster_min_nodes, int *last_grid);
 SFEM_API int sfem_batch_destroy(sfem_batch *batch);
+
+/* ---- serving: a device-resident request loop ------------------------------ */
+
+/* A server runs one persistent kernel that takes assemble-and-solve requests
+ * from a device queue while they keep arriving (continuous batching), for one
+ * element class.  No reference counterpart: the reference solves one mesh per
+ * call.  Requests wait on the host until their device footprint fits the HBM
+ * budget; the sparsity pattern is built once per topology key and kept on
+ * the GPU.  Each request's result is independent of what else is in flight. */
+typedef struct sfem_server sfem_server;
+
+typedef struct {
+    int ndim, function_class, nDof, plane;  /* element class of every request      */
+    int cluster;               /* CTAs working together on one request: 1,2,4,8  */
+    int threads;               /* threads per CTA: 256 or 512                    */
+    double sm_fraction;        /* share of the GPU's CTA slots this server uses  */
+    double hbm_budget_fraction;/* of free HBM at creation, for request buffers   */
+    int64_t hbm_budget_bytes;  /* > 0: explicit budget instead of the fraction   */
+    int max_inflight;          /* requests on the GPU at once (ring capacity)    */
+    double idle_exit_ms;       /* the kernel leaves after this long without work;
+                                  the server relaunches it on the next request   */
+    sfem_solve_opts solve;     /* precision, precond, rtol, maxit, reliable_delta */
+} sfem_server_config;
+
+typedef struct {
+    int status;                /* sfem_status of the request                     */
+    int iterations, refreshes;
+    double relres;
+    double queue_ms;           /* submit -> published to the GPU                 */
+    double gpu_ms;             /* GPU time of the request                        */
+    double total_ms;           /* submit -> result on the host                   */
+    int64_t ndof;
+} sfem_server_result;
+
+typedef struct {
+    int64_t completed, pending, inflight, peak_inflight, kernel_launches;
+    int64_t bytes_in_use, peak_bytes, budget_bytes, topologies;
+    int grid, cluster, last_error;
+} sfem_server_totals;
+
+SFEM_API void sfem_server_config_default(sfem_server_config *cfg);
+SFEM_API int sfem_server_create(int device, const sfem_server_config *cfg, sfem_server **out);
+/* Queue one request (arrays as for sfem_mesh_create / sfem_solve_dirichlet,
+ * host memory, copied before the call returns).  topology_key != 0 shares the
+ * pattern with earlier requests of the same key (IEN/ID may then be NULL once
+ * the first one has been placed); 0 builds it for this request only.
+ * Young: 1 or nEl values; nu: 1 value. */
+SFEM_API int sfem_server_submit(sfem_server *srv, int64_t topology_key, const double *NodeList,
+                                int64_t nNodes, const int64_t *IEN, int64_t nEl, int nen,
+                                const int64_t *ID, const double *Young, int64_t nYoung,
+                                const double *nu, int64_t nNu, const int64_t *fixed_dofs,
+                                int64_t nfix, const double *fixed_vals, int64_t *request_id);
+/* Wait up to timeout_ms (< 0: forever) for a request; on SFEM_OK copies its u
+ * (nDof*nNodes values) and forgets the request.  SFEM_TIMEOUT leaves it queued. */
+SFEM_API int sfem_server_wait(sfem_server *srv, int64_t request_id, double timeout_ms, double *u_out,
+                              int64_t u_len, sfem_server_result *result);
+SFEM_API int sfem_server_info(sfem_server *srv, sfem_server_totals *totals);
+/* Requests still waiting on the host are dropped (SFEM_TIMEOUT); those on the
+ * GPU finish first. */
+SFEM_API int sfem_server_destroy(sfem_server *srv);
 
 #ifdef __cplusplus
 }

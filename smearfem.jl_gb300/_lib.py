@@ -14,9 +14,10 @@ LIB_PATH = os.path.join(PKG, "lib", "libsmearfem_gpu.so")
 
 SFEM_OK, SFEM_BAD_ARG, SFEM_BAD_INDEX, SFEM_SINGULAR_JACOBIAN, SFEM_OOM = 0, 1, 2, 3, 4
 SFEM_NOT_CONVERGED, SFEM_CUDA_ERROR, SFEM_SINGULAR, SFEM_UNSUPPORTED = 5, 6, 7, 8
+SFEM_TIMEOUT = 9
 STATUS_NAMES = {0: "SFEM_OK", 1: "SFEM_BAD_ARG", 2: "SFEM_BAD_INDEX", 3: "SFEM_SINGULAR_JACOBIAN",
                 4: "SFEM_OOM", 5: "SFEM_NOT_CONVERGED", 6: "SFEM_CUDA_ERROR", 7: "SFEM_SINGULAR",
-                8: "SFEM_UNSUPPORTED"}
+                8: "SFEM_UNSUPPORTED", 9: "SFEM_TIMEOUT"}
 MEM_HOST, MEM_DEVICE = 0, 1
 Q1, Q2 = 1, 2
 PLANE_STRESS, PLANE_STRAIN = 0, 1
@@ -51,6 +52,27 @@ class SolveStats(C.Structure):
 class BatchStats(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("refreshes", C.c_int),
                 ("group_ctas", C.c_int), ("relres", C.c_double), ("ms", C.c_double)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("function_class", C.c_int), ("nDof", C.c_int), ("plane", C.c_int),
+                ("cluster", C.c_int), ("threads", C.c_int), ("sm_fraction", C.c_double),
+                ("hbm_budget_fraction", C.c_double), ("hbm_budget_bytes", C.c_int64),
+                ("max_inflight", C.c_int), ("idle_exit_ms", C.c_double), ("solve", SolveOpts)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("refreshes", C.c_int),
+                ("relres", C.c_double), ("queue_ms", C.c_double), ("gpu_ms", C.c_double),
+                ("total_ms", C.c_double), ("ndof", C.c_int64)]
+
+
+class ServerTotals(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("pending", C.c_int64), ("inflight", C.c_int64),
+                ("peak_inflight", C.c_int64), ("kernel_launches", C.c_int64),
+                ("bytes_in_use", C.c_int64), ("peak_bytes", C.c_int64), ("budget_bytes", C.c_int64),
+                ("topologies", C.c_int64), ("grid", C.c_int), ("cluster", C.c_int),
+                ("last_error", C.c_int)]
 
 
 _lib = None
@@ -95,6 +117,13 @@ SIGNATURES = {
     "sfem_batch_destroy": (C.c_int, [P]),
     "sfem_solve_dirichlet": (C.c_int, [P, P, P, I64, P, P, P, C.c_int, C.POINTER(SolveOpts),
                                        C.POINTER(SolveStats)]),
+    "sfem_server_config_default": (None, [C.POINTER(ServerConfig)]),
+    "sfem_server_create": (C.c_int, [C.c_int, C.POINTER(ServerConfig), PP]),
+    "sfem_server_submit": (C.c_int, [P, I64, P, I64, P, I64, C.c_int, P, P, I64, P, I64, P, I64, P,
+                                     I64P]),
+    "sfem_server_wait": (C.c_int, [P, I64, C.c_double, P, I64, C.POINTER(ServerResult)]),
+    "sfem_server_info": (C.c_int, [P, C.POINTER(ServerTotals)]),
+    "sfem_server_destroy": (C.c_int, [P]),
 }
 
 

@@ -87,6 +87,10 @@ def test_no_gpu_fails_loudly(sfem):
         pass
     with pytest.raises(sfem.SfemError):
         sfem.Context(0)
+    with pytest.raises(sfem.SfemError):
+        sfem.Server(ndim=2, nDof=2)
+    with pytest.raises(KeyError):
+        sfem.Server(ndim=2, nDof=2, precision="fp16")
 
 
 def test_missing_library_is_an_error(sfem, monkeypatch, tmp_path):
