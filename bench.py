@@ -513,7 +513,7 @@ def batch_leg(args, pkg, ctx, stream, dist):
             "speedup_vs_plain_fp64": (n_total / (ms * 1e-3)) / (n_total / t_plain)}
 
 
-def _stream(servers, pool, arrivals, which):
+def _stream(srv_all, pool, arrivals, which):
     """Open-loop driver: a thread submits pool[which[i]] at arrivals[i] (s);
     the caller's thread collects results.  Returns per-request records and
     the wall time from the first submission to the last result."""
@@ -529,9 +529,10 @@ def _stream(servers, pool, arrivals, which):
             if d > 0:
                 time.sleep(d)
             p = pool[which[i]]
-            srv = servers[p.ndim]
+            srv = srv_all
             ids[i] = (srv, srv.submit(p.NodeList, p.IEN[: p.n_elem], p.ID, p.Young, p.nu,
-                                      p.fixed_dofs, p.fixed_vals, topology_key=p.ne))
+                                      p.fixed_dofs, p.fixed_vals, topology_key=p.ndim * 100000 + p.ne,
+                                      ndim=p.ndim, nDof=p.ndim, plane=p.plane))
             ready[i].set()
 
     th = threading.Thread(target=submitter, daemon=True)
@@ -547,47 +548,51 @@ def _stream(servers, pool, arrivals, which):
     return recs, t_last - t0
 
 
+def _concurrency(recs):
+    """Mean number of requests on the GPU at once over the stream (device clock)."""
+    iv = [(r["t_claim_ms"], r["t_end_ms"]) for _, _, r in recs]
+    span = max(b for _, b in iv) - min(a for a, _ in iv)
+    return float(sum(b - a for a, b in iv) / span) if span > 0 else 0.0
+
+
 def serve_leg(args, pkg, ctx, dist):
     """Serving workload: an open-loop Poisson stream, 70% plane-strain quads
     n ~ U{32..512}, 30% hexes n ~ U{16..64}, per-element E ~ lognormal(0, 0.5),
     nu ~ U(0.25, 0.45) per request, seeded boundary displacements; one server
-    per element class (2D: 55% of the GPU's CTA slots, 3D: 35%), topology key
-    = mesh size, mixed-precision block-Jacobi PCG.  Requests draw from a pool
+    (one persistent kernel for both element classes), topology key = class and
+    mesh size, mixed-precision block-Jacobi PCG.  Requests draw from a pool
     of distinct meshes, so a repeated request must give the same bits."""
     rng = np.random.default_rng(2005)
     pool = [p for _, p in pkg.meshgen.config5_stream(args.serve_pool)]
     rtol = args.batch_rtol
-    kw = dict(precision="mixed", precond="block_jacobi", rtol=rtol, cluster=4, idle_exit_ms=200.0)
-    servers = {2: pkg.Server(ndim=2, nDof=2, plane="strain", sm_fraction=0.55, **kw),
-               3: pkg.Server(ndim=3, nDof=3, sm_fraction=0.35, **kw)}
+    srv = pkg.Server(precision="mixed", precond="block_jacobi", rtol=rtol, cluster=4, idle_exit_ms=200.0)
     try:
         # warm-up: every pool mesh once (builds and caches each topology's pattern)
-        recs, t_warm = _stream(servers, pool, np.zeros(len(pool)), np.arange(len(pool)))
+        recs, t_warm = _stream(srv, pool, np.zeros(len(pool)), np.arange(len(pool)))
         first = {k: u for k, u, _ in recs}
         # saturation: the offered rate far above capacity
         n = args.serve_requests
         arr = np.cumsum(rng.exponential(1.0 / args.serve_rate, n))
         which = rng.integers(0, len(pool), n)
-        recs, wall = _stream(servers, pool, arr, which)
+        recs, wall = _stream(srv, pool, arr, which)
         lat = np.array([r["total_ms"] for _, _, r in recs])
         gpu = np.array([r["gpu_ms"] for _, _, r in recs])
         dofs = float(sum(r["ndof"] for _, _, r in recs))
         same = sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs)
         capacity = n / wall
-        peak = {d: servers[d].info() for d in servers}
+        peak = srv.info()
         # below capacity: latency without a backlog
         m = max(20, min(120, int(capacity * 8)))
         rate = 0.5 * capacity
         arr2 = np.cumsum(rng.exponential(1.0 / rate, m))
         which2 = rng.integers(0, len(pool), m)
-        recs2, wall2 = _stream(servers, pool, arr2, which2)
+        recs2, wall2 = _stream(srv, pool, arr2, which2)
         lat2 = np.array([r["total_ms"] for _, _, r in recs2])
         same += sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs2)
         statuses_ok = sum(r["status"] == 0 for _, _, r in recs + recs2)
-        info = {d: servers[d].info() for d in servers}
+        info = srv.info()
     finally:
-        for s_ in servers.values():
-            s_.close()
+        srv.close()
     # error against tight FP64 solves, and the plain FP64 GPU path, on a sample of the pool
     sample = list(range(0, len(pool), max(1, len(pool) // 16)))
     errs, t_plain, dof_plain = [], 0.0, 0
@@ -612,10 +617,9 @@ def serve_leg(args, pkg, ctx, dist):
             "below_capacity": {"rate": rate, "requests": m, "solves_per_s": m / wall2,
                                "latency_ms": {"p50": pct(lat2, 50), "p99": pct(lat2, 99)}},
             "repeat_bitwise_identical": f"{same}/{n + m}", "statuses_ok": int(statuses_ok),
-            "warmup_s": t_warm, "peak_inflight": {d: peak[d]["peak_inflight"] for d in peak},
-            "peak_bytes": {d: info[d]["peak_bytes"] for d in info},
-            "kernel_launches": {d: info[d]["kernel_launches"] for d in info},
-            "grid": {d: [info[d]["grid"], info[d]["cluster"]] for d in info},
+            "warmup_s": t_warm, "peak_inflight": peak["peak_inflight"], "peak_bytes": info["peak_bytes"],
+            "kernel_launches": info["kernel_launches"], "grid_ctas": info["grid"], "cluster": info["cluster"],
+            "gpu_concurrency": _concurrency(recs),
             "rel_err_max_sample": max(errs),
             "plain_fp64_gpu": {"dof_per_s": dof_plain / t_plain,
                                "path": "single-mesh API per request: FP64 Jacobi-PCG (solve only)"},

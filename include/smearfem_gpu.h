@@ -297,18 +297,20 @@ SFEM_API int sfem_batch_destroy(sfem_batch *batch);
 /* ---- serving: a device-resident request loop ------------------------------ */
 
 /* A server runs one persistent kernel that takes assemble-and-solve requests
- * from a device queue while they keep arriving (continuous batching), for one
- * element class.  No reference counterpart: the reference solves one mesh per
- * call.  Requests wait on the host until their device footprint fits the HBM
- * budget; the sparsity pattern is built once per topology key and kept on
- * the GPU.  Each request's result is independent of what else is in flight. */
+ * from a device queue while they keep arriving (continuous batching).  Each
+ * request names its own element class (any that sfem_mesh_create accepts)
+ * and plane law; requests of every class share the one kernel.  No reference
+ * counterpart: the reference solves one mesh per call.  Requests wait on the
+ * host until their device footprint fits the HBM budget; the sparsity
+ * pattern is built once per topology key and kept on the GPU.  Each
+ * request's result is independent of what else is in flight. */
 typedef struct sfem_server sfem_server;
 
 typedef struct {
-    int ndim, function_class, nDof, plane;  /* element class of every request      */
     int cluster;               /* CTAs working together on one request: 1,2,4,8  */
     int threads;               /* threads per CTA: 256 or 512                    */
-    double sm_fraction;        /* share of the GPU's CTA slots this server uses  */
+    double sm_fraction;        /* share of the GPU's CTA slots the kernel uses;
+                                  the rest runs the pattern builds of new keys   */
     double hbm_budget_fraction;/* of free HBM at creation, for request buffers   */
     int64_t hbm_budget_bytes;  /* > 0: explicit budget instead of the fraction   */
     int max_inflight;          /* requests on the GPU at once (ring capacity)    */
@@ -325,6 +327,9 @@ typedef struct {
     double gpu_ms;             /* GPU time of the request                        */
     double total_ms;           /* submit -> result on the host                   */
     int64_t ndof;
+    double t_claim_ms, t_end_ms; /* GPU clock (%globaltimer, ms) when a group took
+                                  the request and when it finished it          */
+    int smid;                  /* SM of the first CTA of that group              */
 } sfem_server_result;
 
 typedef struct {
@@ -335,18 +340,17 @@ typedef struct {
 
 SFEM_API void sfem_server_config_default(sfem_server_config *cfg);
 SFEM_API int sfem_server_create(int device, const sfem_server_config *cfg, sfem_server **out);
-/* Queue one request (arrays as for sfem_mesh_create / sfem_solve_dirichlet,
- * host memory, copied before the call returns).  topology_key != 0 shares the
- * pattern with earlier requests of the same key (IEN/ID may then be NULL once
- * the first one has been placed); 0 builds it for this request only.
- * Young: 1 or nEl values; nu: 1 value. */
-SFEM_API int sfem_server_submit(sfem_server *srv, int64_t topology_key, const double *NodeList,
-                                int64_t nNodes, const int64_t *IEN, int64_t nEl, int nen,
-                                const int64_t *ID, const double *Young, int64_t nYoung,
-                                const double *nu, int64_t nNu, const int64_t *fixed_dofs,
+/* Queue one request: element class and arrays as for sfem_mesh_create and
+ * sfem_solve_dirichlet (host memory, copied before the call returns; nen
+ * follows from the class).  topology_key != 0 shares the pattern with earlier
+ * requests of the same key, which must have the same class and sizes (IEN/ID
+ * may then be NULL); 0 builds it for this request only.  Young: 1 or nEl
+ * values; nu: 1 value. */
+SFEM_API int sfem_server_submit(sfem_server *srv, int ndim, int function_class, int nDof, int plane,
+                                int64_t topology_key, const double *NodeList, int64_t nNodes,
+                                const int64_t *IEN, int64_t nEl, const int64_t *ID, const double *Young,
+                                int64_t nYoung, const double *nu, int64_t nNu, const int64_t *fixed_dofs,
                                 int64_t nfix, const double *fixed_vals, int64_t *request_id);
-/* Wait up to timeout_ms (< 0: forever) for a request; on SFEM_OK copies its u
- * (nDof*nNodes values) and forgets the request.  SFEM_TIMEOUT leaves it queued. */
 SFEM_API int sfem_server_wait(sfem_server *srv, int64_t request_id, double timeout_ms, double *u_out,
                               int64_t u_len, sfem_server_result *result);
 SFEM_API int sfem_server_info(sfem_server *srv, sfem_server_totals *totals);

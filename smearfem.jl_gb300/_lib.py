@@ -55,8 +55,7 @@ class BatchStats(C.Structure):
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("ndim", C.c_int), ("function_class", C.c_int), ("nDof", C.c_int), ("plane", C.c_int),
-                ("cluster", C.c_int), ("threads", C.c_int), ("sm_fraction", C.c_double),
+    _fields_ = [("cluster", C.c_int), ("threads", C.c_int), ("sm_fraction", C.c_double),
                 ("hbm_budget_fraction", C.c_double), ("hbm_budget_bytes", C.c_int64),
                 ("max_inflight", C.c_int), ("idle_exit_ms", C.c_double), ("solve", SolveOpts)]
 
@@ -64,7 +63,8 @@ class ServerConfig(C.Structure):
 class ServerResult(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("refreshes", C.c_int),
                 ("relres", C.c_double), ("queue_ms", C.c_double), ("gpu_ms", C.c_double),
-                ("total_ms", C.c_double), ("ndof", C.c_int64)]
+                ("total_ms", C.c_double), ("ndof", C.c_int64), ("t_claim_ms", C.c_double),
+                ("t_end_ms", C.c_double), ("smid", C.c_int)]
 
 
 class ServerTotals(C.Structure):
@@ -119,8 +119,8 @@ SIGNATURES = {
                                        C.POINTER(SolveStats)]),
     "sfem_server_config_default": (None, [C.POINTER(ServerConfig)]),
     "sfem_server_create": (C.c_int, [C.c_int, C.POINTER(ServerConfig), PP]),
-    "sfem_server_submit": (C.c_int, [P, I64, P, I64, P, I64, C.c_int, P, P, I64, P, I64, P, I64, P,
-                                     I64P]),
+    "sfem_server_submit": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, I64, P, I64, P, I64, P,
+                                     P, I64, P, I64, P, I64, P, I64P]),
     "sfem_server_wait": (C.c_int, [P, I64, C.c_double, P, I64, C.POINTER(ServerResult)]),
     "sfem_server_info": (C.c_int, [P, C.POINTER(ServerTotals)]),
     "sfem_server_destroy": (C.c_int, [P]),

@@ -42,7 +42,7 @@ struct sfem_batch {
     bool buffers = false;
     double *kbuf = nullptr, *val64 = nullptr, *ud = nullptr, *b64 = nullptr, *x64 = nullptr, *q64 = nullptr;
     float *val32 = nullptr;
-    void *vecT = nullptr;         // 5 work vectors of the CG type + preconditioner
+    void *vecT = nullptr;         // 6 work vectors of the CG type + preconditioner
     unsigned char *fixed = nullptr, *gfixed = nullptr;
     double *E = nullptr, *nu = nullptr, *fvals = nullptr, *u = nullptr;
     int64_t *fdofs = nullptr, *fix_off_dev = nullptr;
@@ -60,9 +60,10 @@ using namespace sfem_dev;
 
 template <int NDIM, int NEN, int NGP, int B, bool MIXED>
 __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
-    __shared__ double red[64];
-    __shared__ double xch[2];
+    __shared__ double red[128];  // two halves, alternating (block_sum2)
+    __shared__ double xch[4];
     __shared__ int s_flag, s_mesh;
+    constexpr int WF = (NDIM == 2 && NEN == 4 && B == 2) ? 9 : 0;  // pipelined 9-slab slices of 2D Q1 elasticity
     const int tid = threadIdx.x;
     cgrp::cluster_group cl = cgrp::this_cluster();
     // 1. large meshes: the whole cluster works on one mesh
@@ -72,7 +73,7 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = *cl.map_shared_rank(&s_mesh, 0);
         cl.sync();
         if (q >= a.nbig) break;
-        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED>(ClusterGroup(), tab, a, a.order[q], red, xch, &s_flag);
+        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED, 4, WF>(ClusterGroup(), tab, a, a.order[q], red, xch, &s_flag);
         cl.sync();
     }
     // 2. small meshes: every CTA on its own
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = (int64_t)a.nbig + s_mesh;
         __syncthreads();
         if (q >= a.nmesh) break;
-        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED>(SoloGroup(), tab, a, a.order[q], red, xch, &s_flag);
+        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED, 4, WF>(SoloGroup(), tab, a, a.order[q], red, xch, &s_flag);
         __syncthreads();
     }
     cl.sync();  // peers may still read this CTA's shared memory until every CTA is done
@@ -362,7 +363,7 @@ static int batch_buffers(sfem_ctx *ctx, sfem_batch *bt) {
     SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->b64, sizeof(double) * nd, "batch rhs"));
     SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->x64, sizeof(double) * nd, "batch x"));
     SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->q64, sizeof(double) * nd, "batch q64"));
-    SFEM_TRY(sfem_dalloc(ctx, &bt->vecT, tsz * (5 * nd + m->nN * b * b), "batch CG vectors"));
+    SFEM_TRY(sfem_dalloc(ctx, &bt->vecT, tsz * (6 * nd + m->nN * b * b), "batch CG vectors"));
     SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->fixed, nd, "batch mask"));
     SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->gfixed, bt->total_dofs + 1, "batch global mask"));
     SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->u, sizeof(double) * (bt->total_dofs + 1), "batch u"));

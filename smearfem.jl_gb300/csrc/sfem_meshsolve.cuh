@@ -101,7 +101,7 @@ struct BatchArgs {
     float *val32;
     unsigned char *fixed, *gfixed;
     double *ud, *b64, *x64, *q64;
-    void *vecT;      // x, r, z, p, q (type T, nd each) then minv (nN * b * b)
+    void *vecT;      // x, r, z, p, q, p' (type T, nd each) then minv (nN * b * b)
     int64_t nd;
     double *u_out;
     int64_t u_len;   // entries of u_out (zeroed by the serving kernel)
@@ -133,8 +133,12 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // CTA-wide sums of (a, b) in a fixed order, returned to every thread.
-__device__ __forceinline__ double2 block_sum2(double a, double b, double *sh) {
+// Successive calls alternate between the two halves of `sh` (128 doubles,
+// half = ph & 1): a half is written again only after every thread has
+// passed the barrier of the call in between, so no closing barrier is needed.
+__device__ __forceinline__ double2 block_sum2(double a, double b, double *sh, int ph) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    sh += 64 * (ph & 1);
     a = warp_sum_d(a);
     b = warp_sum_d(b);
     if (lane == 0) {
@@ -147,46 +151,155 @@ __device__ __forceinline__ double2 block_sum2(double a, double b, double *sh) {
         x += sh[w];
         y += sh[32 + w];
     }
-    __syncthreads();
     return make_double2(x, y);
 }
 
-// y = (mask ? 0 : K x) over the mesh's slices; returns this thread's x.y share.
-// Rows at or beyond `rend` (the padding that rounds a mesh up to whole
-// slices) are neither written nor counted: their vector entries are unset.
-// Slices sfirst, sfirst + sstride, ... below s1 (one warp each).
-template <typename T, int B>
-__device__ double grp_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val,
-                           int64_t sfirst, int64_t s1, int64_t sstride, int64_t rend, const T *__restrict__ x,
-                           T *__restrict__ y, const unsigned char *__restrict__ fixed, bool masked) {
+// Entry idx of the multiplied vector: x itself, or with FUSE_P the CG search
+// direction z + beta * x formed on the fly (x = the previous direction).
+template <bool FUSE_P, typename T>
+__device__ __forceinline__ T spmv_operand(const T *__restrict__ x, const T *__restrict__ z, T beta, int64_t idx) {
+    if constexpr (FUSE_P) return fma(beta, x[idx], z[idx]);
+    else return x[idx];
+}
+
+// y = (mask ? 0 : K v) over the mesh's slices, v = x or (FUSE_P) z + beta x;
+// returns this thread's v.y share.  With FUSE_P this thread's rows of v are
+// stored to pnew.  Rows at or beyond `rend` (the padding that rounds a mesh
+// up to whole slices) are neither written nor counted: their vector entries
+// are unset.  Slices sfirst, sfirst + sstride, ... below s1 (one warp each).
+//
+// A resident CTA or two per SM leave few warps to hide memory latency, so
+// the loads are batched: a thread keeps U slabs in flight, loads its own
+// row's entries up front and the slice extents ahead of use.  With W > 0,
+// slices exactly W slabs wide (the interior of a structured 2D Q1 mesh: 9)
+// take a pipelined path: their column indices were loaded while the
+// previous slice was multiplied, so values, gathers and the next slice's
+// indices all go out together -- one memory round trip per slice.  K and
+// its column indices are read once per product and are loaded with the
+// streaming hint, which leaves the L1 to the gathered vector entries.  The
+// products are added in slab order on every path, so sums do not depend on
+// U, W or the path taken.
+template <typename T, int B, bool FUSE_P, int U, int W = 0>
+__device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col,
+                                           const T *__restrict__ val, int64_t sfirst, int64_t s1, int64_t sstride,
+                                           int64_t rend, const T *__restrict__ x, const T *__restrict__ z, T beta,
+                                           T *__restrict__ pnew, T *__restrict__ y, const unsigned char *__restrict__ fixed,
+                                           bool masked) {
+    constexpr int WP = W > 0 ? W : 1;
     const int lane = threadIdx.x & 31;
     double dot = 0.0;
+    int64_t k0 = 0, k1 = 0, nk0 = 0, nk1 = 0;  // this slice's and the next slice's extents
+    if (sfirst < s1) {
+        k0 = sliceptr[sfirst];
+        k1 = sliceptr[sfirst + 1];
+    }
+    if (sfirst + sstride < s1) {
+        nk0 = sliceptr[sfirst + sstride];
+        nk1 = sliceptr[sfirst + sstride + 1];
+    }
+    int cn[WP];  // column indices of this slice when it is exactly W wide
+    if constexpr (W > 0) {
+        if (k1 - k0 == W) {
+#pragma unroll
+            for (int u = 0; u < W; ++u) cn[u] = __ldcs(col + (k0 + u) * 32 + lane);
+        }
+    }
     for (int64_t s = sfirst; s < s1; s += sstride) {
         const int64_t r = s * 32 + lane;
-        const int64_t k0 = sliceptr[s], k1 = sliceptr[s + 1];
+        const bool own = r < rend;
+        int64_t nnk0 = 0, nnk1 = 0;  // two slices ahead
+        if (s + 2 * sstride < s1) {
+            nnk0 = sliceptr[s + 2 * sstride];
+            nnk1 = sliceptr[s + 2 * sstride + 1];
+        }
+        T pd[B];
+        bool fx[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            pd[i] = own ? spmv_operand<FUSE_P>(x, z, beta, r * B + i) : T(0);
+            fx[i] = own && masked && fixed[r * B + i];
+        }
         T acc[B];
 #pragma unroll
         for (int i = 0; i < B; ++i) acc[i] = T(0);
-#pragma unroll 2
-        for (int64_t k = k0; k < k1; ++k) {
-            const int c = col[k * 32 + lane];
-            T v[B * B];
+        int ncn[WP];
+        if (W > 0 && k1 - k0 == W) {
+            T v[WP][B * B], g[WP][B];
 #pragma unroll
-            for (int e = 0; e < B * B; ++e) v[e] = val[(k * B * B + e) * 32 + lane];
+            for (int u = 0; u < WP; ++u)
 #pragma unroll
-            for (int i = 0; i < B; ++i)
+                for (int e = 0; e < B * B; ++e) v[u][e] = __ldcs(val + ((k0 + u) * B * B + e) * 32 + lane);
 #pragma unroll
-                for (int j = 0; j < B; ++j) acc[i] = fma(v[i * B + j], x[(int64_t)c * B + j], acc[i]);
+            for (int u = 0; u < WP; ++u)
+#pragma unroll
+                for (int j = 0; j < B; ++j) g[u][j] = spmv_operand<FUSE_P>(x, z, beta, (int64_t)cn[u] * B + j);
+            if (nk1 - nk0 == W) {
+#pragma unroll
+                for (int u = 0; u < WP; ++u) ncn[u] = __ldcs(col + (nk0 + u) * 32 + lane);
+            }
+#pragma unroll
+            for (int u = 0; u < WP; ++u)
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) acc[i] = fma(v[u][i * B + j], g[u][j], acc[i]);
+        } else {
+            if (W > 0 && nk1 - nk0 == W) {
+#pragma unroll
+                for (int u = 0; u < WP; ++u) ncn[u] = __ldcs(col + (nk0 + u) * 32 + lane);
+            }
+            int64_t k = k0;
+            for (; k + U <= k1; k += U) {
+                int c[U];
+                T v[U][B * B], g[U][B];
+#pragma unroll
+                for (int u = 0; u < U; ++u) c[u] = __ldcs(col + (k + u) * 32 + lane);
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int e = 0; e < B * B; ++e) v[u][e] = __ldcs(val + ((k + u) * B * B + e) * 32 + lane);
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) g[u][j] = spmv_operand<FUSE_P>(x, z, beta, (int64_t)c[u] * B + j);
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int i = 0; i < B; ++i)
+#pragma unroll
+                        for (int j = 0; j < B; ++j) acc[i] = fma(v[u][i * B + j], g[u][j], acc[i]);
+            }
+            for (; k < k1; ++k) {
+                const int c = __ldcs(col + k * 32 + lane);
+                T v[B * B], g[B];
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) v[e] = __ldcs(val + (k * B * B + e) * 32 + lane);
+#pragma unroll
+                for (int j = 0; j < B; ++j) g[j] = spmv_operand<FUSE_P>(x, z, beta, (int64_t)c * B + j);
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) acc[i] = fma(v[i * B + j], g[j], acc[i]);
+            }
         }
-        if (r < rend) {
+        if (own) {
 #pragma unroll
             for (int i = 0; i < B; ++i) {
                 const int64_t d = r * B + i;
-                const T out = (masked && fixed[d]) ? T(0) : acc[i];
+                if constexpr (FUSE_P) pnew[d] = pd[i];
+                const T out = fx[i] ? T(0) : acc[i];
                 y[d] = out;
-                dot += (double)x[d] * (double)out;
+                dot += (double)pd[i] * (double)out;
             }
         }
+        if constexpr (W > 0) {
+#pragma unroll
+            for (int u = 0; u < WP; ++u) cn[u] = ncn[u];
+        }
+        k0 = nk0;
+        k1 = nk1;
+        nk0 = nnk0;
+        nk1 = nnk1;
     }
     return dot;
 }
@@ -196,8 +309,8 @@ struct SoloGroup {
     __device__ __forceinline__ int rank() const { return 0; }
     __device__ __forceinline__ int size() const { return 1; }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
-    __device__ double2 sum2(double a, double b, double *red, double *) const { return block_sum2(a, b, red); }
-    __device__ int max_flag(int *flag) const {
+    __device__ __forceinline__ double2 sum2(double a, double b, double *red, double *, int ph) const { return block_sum2(a, b, red, ph); }
+    __device__ __forceinline__ int max_flag(int *flag) const {
         __syncthreads();
         const int f = *flag;
         __syncthreads();
@@ -212,9 +325,11 @@ struct ClusterGroup {
     __device__ __forceinline__ int rank() const { return (int)cgrp::this_cluster().block_rank(); }
     __device__ __forceinline__ int size() const { return (int)cgrp::this_cluster().num_blocks(); }
     __device__ __forceinline__ void sync() const { cgrp::this_cluster().sync(); }
-    __device__ double2 sum2(double a, double b, double *red, double *xch) const {
-        const double2 p = block_sum2(a, b, red);
+    // xch: 4 doubles, alternating halves like block_sum2's buffer (one cluster barrier per call)
+    __device__ __forceinline__ double2 sum2(double a, double b, double *red, double *xch, int ph) const {
+        const double2 p = block_sum2(a, b, red, ph);
         cgrp::cluster_group cl = cgrp::this_cluster();
+        xch += 2 * (ph & 1);
         if (threadIdx.x == 0) {
             xch[0] = p.x;
             xch[1] = p.y;
@@ -226,10 +341,9 @@ struct ClusterGroup {
             x += rx[0];
             y += rx[1];
         }
-        cl.sync();
         return make_double2(x, y);
     }
-    __device__ int max_flag(int *flag) const {
+    __device__ __forceinline__ int max_flag(int *flag) const {
         cgrp::cluster_group cl = cgrp::this_cluster();
         cl.sync();
         int f = 0;
@@ -240,8 +354,11 @@ struct ClusterGroup {
 };
 
 // Assemble and solve mesh `mb` with group G (a CTA or a cluster).
-template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED>
-__device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
+// UF: slabs in flight per thread in the CG loop's SpMV, WF: slice width of
+// its pipelined path (0: none), NV: nodes per thread and step of the vector
+// update.  The register budget of the calling kernel decides what fits.
+template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF = 4, int WF = 0, int NVF = 1>
+__device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
                              int *s_flag) {
     using T = typename std::conditional<MIXED, float, double>::type;
     constexpr int GS = NEN * NDIM + 1;
@@ -256,8 +373,9 @@ __device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArg
     double *sG = smem + (int64_t)grp * (NGP * 32 * GS + NGP * 32);
     double *sW = sG + NGP * 32 * GS;
     T *xv = (T *)a.vecT;
-    T *rv = xv + a.nd, *zv = rv + a.nd, *pv = zv + a.nd, *qv = pv + a.nd;
-    T *minv = qv + a.nd;  // [nN][B][B]
+    T *rv = xv + a.nd, *zv = rv + a.nd, *pv = zv + a.nd, *qv = pv + a.nd, *pw = qv + a.nd;  // pv/pw: directions, alternating
+    T *minv = pw + a.nd;  // [nN][B][B]
+    int ph = 0;           // parity of the reduction buffers
     const T *valT = MIXED ? (const T *)a.val32 : (const T *)a.val64;
     const BatchMesh M = a.meshes[mb];
     unsigned long long t_start = 0;
@@ -481,7 +599,8 @@ __device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArg
                 atomicMax(s_flag, (int)SFEM_SINGULAR);  // a free DOF with no row in K
         }
         // b = -K q_d on the free DOFs (FP64)
-        grp_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.ud, a.q64, a.fixed, false);
+        grp_spmv<double, B, false, 2>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.ud, nullptr, 0.0,
+                                   nullptr, a.q64, a.fixed, false);
         G.sync();
         for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) a.b64[d] = a.fixed[d] ? 0.0 : -a.q64[d];
 
@@ -582,7 +701,7 @@ __device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArg
                     prz += (double)(r[i] * zi);
                 }
             }
-            const double2 t = G.sum2(prz, pbb, red, xch);
+            const double2 t = G.sum2(prz, pbb, red, xch, ph++);
             rz = t.x;
             bb = t.y;
         }
@@ -591,37 +710,66 @@ __device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArg
         int it = 0, refreshes = 0, status = G.max_flag(s_flag);
         bool done = status != SFEM_OK || !(bb > 0.0);
         while (!done) {
-            // p = z + beta p
-            for (int64_t d = n0 * B + gt; d < n1 * B; d += gstride) pv[d] = fma((T)beta, pv[d], zv[d]);
-            G.sync();
-            double pq = grp_spmv<T, B>(a.sliceptr, a.col, valT, M.slice0 + gw, M.slice1, gnw, n1, pv, qv, a.fixed, true);
-            pq = G.sum2(pq, 0.0, red, xch).x;
+            // q = K p with p = z + beta p_prev formed inside the SpMV (stored to pw)
+            double pq = grp_spmv<T, B, true, (sizeof(T) == 8 ? 2 : UF), (sizeof(T) == 8 ? 0 : WF)>(
+                a.sliceptr, a.col, valT, M.slice0 + gw, M.slice1, gnw, n1, pv, zv,
+                                             (T)beta, pw, qv, a.fixed, true);
+            {
+                T *t = pv;  // pv: the current direction
+                pv = pw;
+                pw = t;
+            }
+            pq = G.sum2(pq, 0.0, red, xch, ph++).x;
             if (!(pq > 0.0)) {
                 status = SFEM_SINGULAR;
                 break;
             }
             const T alpha = (T)(rz / pq);
             double prz = 0.0, prr = 0.0;
-            for (int64_t node = n0 + gt; node < n1; node += gstride) {
-                T r[B];
+            // x += alpha p, r -= alpha q, z = M^-1 r; NV nodes per thread per step (loads first)
+            constexpr int NV = sizeof(T) == 8 ? 1 : NVF;
+            for (int64_t nb = n0 + gt; nb < n1; nb += NV * gstride) {
+                T P[NV][B], X[NV][B], Q[NV][B], R[NV][B], Mi[NV][B * B];
 #pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    const int64_t d = node * B + i;
-                    xv[d] = fma(alpha, pv[d], xv[d]);
-                    r[i] = fma(-alpha, qv[d], rv[d]);
-                    rv[d] = r[i];
-                    prr += (double)(r[i] * r[i]);
+                for (int v = 0; v < NV; ++v) {
+                    const int64_t node = nb + v * gstride;
+                    if (node < n1) {
+#pragma unroll
+                        for (int i = 0; i < B; ++i) {
+                            const int64_t d = node * B + i;
+                            P[v][i] = pv[d];
+                            X[v][i] = xv[d];
+                            Q[v][i] = qv[d];
+                            R[v][i] = rv[d];
+                        }
+#pragma unroll
+                        for (int e = 0; e < B * B; ++e) Mi[v][e] = minv[node * B * B + e];
+                    }
                 }
 #pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    T zi = T(0);
+                for (int v = 0; v < NV; ++v) {
+                    const int64_t node = nb + v * gstride;
+                    if (node < n1) {
 #pragma unroll
-                    for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
-                    zv[node * B + i] = zi;
-                    prz += (double)(r[i] * zi);
+                        for (int i = 0; i < B; ++i) {
+                            const int64_t d = node * B + i;
+                            xv[d] = fma(alpha, P[v][i], X[v][i]);
+                            R[v][i] = fma(-alpha, Q[v][i], R[v][i]);
+                            rv[d] = R[v][i];
+                            prr += (double)(R[v][i] * R[v][i]);
+                        }
+#pragma unroll
+                        for (int i = 0; i < B; ++i) {
+                            T zi = T(0);
+#pragma unroll
+                            for (int j = 0; j < B; ++j) zi = fma(Mi[v][i * B + j], R[v][j], zi);
+                            zv[node * B + i] = zi;
+                            prz += (double)(R[v][i] * zi);
+                        }
+                    }
                 }
             }
-            const double2 t = G.sum2(prz, prr, red, xch);
+            const double2 t = G.sum2(prz, prr, red, xch, ph++);
             ++it;
             const double rz_prev = rz;
             rz = t.x;
@@ -647,8 +795,8 @@ __device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArg
                     xv[d] = T(0);
                 }
                 G.sync();
-                grp_spmv<double, B>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.x64, a.q64,
-                                    a.fixed, true);
+                grp_spmv<double, B, false, 2>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, a.x64,
+                                           nullptr, 0.0, nullptr, a.q64, a.fixed, true);
                 G.sync();
                 double frz = 0.0, frr = 0.0;
                 for (int64_t node = n0 + gt; node < n1; node += gstride) {
@@ -670,7 +818,7 @@ __device__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArg
                         frz += (double)(r[i] * zi);
                     }
                 }
-                const double2 f = G.sum2(frz, frr, red, xch);
+                const double2 f = G.sum2(frz, frr, red, xch, ph++);
                 ++refreshes;
                 rz = f.x;
                 rr = f.y;

@@ -24,7 +24,9 @@
 // the kernel keeps running, so after every claim each thread executes a
 // system-scope acquire fence: it drops L1 lines that may still hold a
 // recycled buffer's old contents.
+#include <algorithm>
 #include <atomic>
+#include <initializer_list>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -39,12 +41,34 @@ namespace {
 
 using namespace sfem_dev;
 
+// Element classes one serving kernel handles; a request names its own.
+enum ServeClass { CLS_Q1_2D_SCALAR = 0, CLS_Q1_2D_ELASTIC, CLS_Q1_3D_SCALAR, CLS_Q1_3D_ELASTIC, CLS_Q2_2D_SCALAR,
+                  NUM_CLASSES };
+
+int serve_class(int ndim, int fclass, int b) {
+    if (fclass == SFEM_Q2) return (ndim == 2 && b == 1) ? CLS_Q2_2D_SCALAR : -1;
+    if (fclass != SFEM_Q1) return -1;
+    if (ndim == 2) return b == 1 ? CLS_Q1_2D_SCALAR : (b == 2 ? CLS_Q1_2D_ELASTIC : -1);
+    if (ndim == 3) return b == 1 ? CLS_Q1_3D_SCALAR : (b == 3 ? CLS_Q1_3D_ELASTIC : -1);
+    return -1;
+}
+
+// Shape-function tables: 2D Q1, 3D Q1, 2D Q2.
+struct ServeTables {
+    ElemTableB t[3];
+};
+
 struct ServeDesc {
     BatchArgs args;
     BatchMesh mesh;
     long long seq;
     int slot;
-    int pad;
+    int cls;  // ServeClass
+};
+
+struct ServeTrace {
+    long long t_claim, t_end;  // %globaltimer (ns) at claim and at completion
+    int smid, pad;             // SM of the group's first CTA
 };
 
 struct ServeCtl {
@@ -56,6 +80,8 @@ struct ServeCtl {
     const int *stop;               // mapped host: stop request
     long long idle_ns;             // leave after this long without work
     int *exit_reason;              // mapped host: 1 idle, 2 stop
+    ServeTrace *trace;             // mapped host: per slot, when and where the request ran
+    unsigned long long *state;     // device: idle / started groups and CLOSING (zeroed per launch)
 };
 
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -80,36 +106,84 @@ __device__ __forceinline__ void st_release_sys(long long *p, long long v) {
     asm volatile("st.release.sys.global.s64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Claim the next published descriptor; -1 after idle_ns without work, -2 on stop.
+// The kernel leaves collectively: a group that has found no work for idle_ns
+// counts itself idle, and once every started group is idle one of them sets
+// CLOSING; from then on no group takes work and all leave.  (A group leaving
+// alone would let the kernel run on with fewer groups, and the host relaunches
+// only a kernel that has ended.)  Groups that start after CLOSING leave at
+// once, so the resident groups never wait for one that is not resident.
+// State word: bits 0-23 idle groups, 24-47 started groups, 63 CLOSING.
+constexpr unsigned long long IDLE_ONE = 1ull, STARTED_ONE = 1ull << 24, CLOSING = 1ull << 63;
+constexpr unsigned long long COUNT_MASK = (1ull << 24) - 1;
+
+__device__ __forceinline__ bool all_idle(unsigned long long v) {
+    return (v & COUNT_MASK) == ((v >> 24) & COUNT_MASK);
+}
+
+// Claim the next published descriptor; -1 when the kernel closes for lack of
+// work, -2 on stop.  Every wait here ends: the host's stop flag, the work of
+// the busy groups (bounded by maxit) and the idle deadline bound it.
 __device__ long long claim(const ServeCtl &c) {
-    const unsigned long long t0 = gtimer();
+    unsigned long long t0 = gtimer();
     unsigned ns = 256;
+    bool idle = false;
     for (;;) {
         if (ld_acquire_sys_i(c.stop)) return -2;
         const long long t = ld_acquire_sys(c.tail);
         const unsigned long long h = atomicAdd(c.head, 0ull);
         if ((long long)h < t) {
+            if (idle) {  // rejoin the busy groups unless the kernel is closing
+                unsigned long long v = atomicAdd(c.state, 0ull);
+                for (;;) {
+                    if (v & CLOSING) return -1;
+                    const unsigned long long w = atomicCAS(c.state, v, v - IDLE_ONE);
+                    if (w == v) break;
+                    v = w;
+                }
+                idle = false;
+                t0 = gtimer();
+            }
             if (atomicCAS(c.head, h, h + 1) == h) return (long long)h;
             continue;  // another group took it: retry at once
         }
-        if ((long long)(gtimer() - t0) > c.idle_ns) return -1;
+        if (!idle) {
+            if ((long long)(gtimer() - t0) > c.idle_ns) {
+                const unsigned long long v = atomicAdd(c.state, IDLE_ONE) + IDLE_ONE;
+                idle = true;
+                if (!(v & CLOSING) && all_idle(v)) atomicCAS(c.state, v, v | CLOSING);
+            }
+        } else {
+            const unsigned long long v = atomicAdd(c.state, 0ull);
+            if (v & CLOSING) return -1;
+            if (all_idle(v)) atomicCAS(c.state, v, v | CLOSING);
+        }
         __nanosleep(ns);
         ns = ns < 8192 ? 2 * ns : 8192;
     }
 }
 
-template <int NDIM, int NEN, int NGP, int B, bool MIXED>
-__global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1))
-k_serve(const __grid_constant__ ElemTableB tab, const __grid_constant__ ServeCtl c) {
-    __shared__ double red[64];
-    __shared__ double xch[2];
+// One group (a thread-block cluster) per request; any element class.
+template <bool MIXED>
+__global__ void __launch_bounds__(512, 1) k_serve(const __grid_constant__ ServeTables tabs, const __grid_constant__ ServeCtl c) {
+    __shared__ double red[128];  // two halves, alternating (block_sum2)
+    __shared__ double xch[4];
     __shared__ int s_flag;
     __shared__ long long s_idx;
     __shared__ __align__(16) BatchArgs s_args;
     cgrp::cluster_group cl = cgrp::this_cluster();
     const int tid = threadIdx.x;
+    long long t_claim = 0;
+    bool joined = false;
     for (;;) {
-        if (cl.block_rank() == 0 && tid == 0) s_idx = claim(c);
+        if (cl.block_rank() == 0 && tid == 0) {
+            bool closed = false;
+            if (!joined) {  // count this group as started, unless the kernel already closes
+                joined = true;
+                closed = (atomicAdd(c.state, STARTED_ONE) & CLOSING) != 0;
+            }
+            s_idx = closed ? -1 : claim(c);
+            t_claim = (long long)gtimer();
+        }
         cl.sync();
         const long long idx = *cl.map_shared_rank(&s_idx, 0);
         cl.sync();
@@ -129,12 +203,40 @@ k_serve(const __grid_constant__ ElemTableB tab, const __grid_constant__ ServeCtl
             for (int64_t i = (int64_t)cl.block_rank() * blockDim.x + tid; i < nu; i += (int64_t)cl.num_blocks() * blockDim.x)
                 s_args.u_out[i] = 0.0;
         }
-        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED>(ClusterGroup(), tab, s_args, 0, red, xch, &s_flag);
+        // Unroll choices per class: the two elasticity classes get the wide SpMV
+        // (the 2D one with its pipelined 9-slab path); the scalar ones stay
+        // narrow, which keeps the shared kernel's register allocation free of spills.
+        const ClusterGroup G;
+        switch (__ldcg(&d->cls)) {
+            case CLS_Q1_2D_SCALAR:
+                process_mesh<ClusterGroup, 2, 4, 4, 1, MIXED, 4, 0, 1>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
+                break;
+            case CLS_Q1_2D_ELASTIC:
+                process_mesh<ClusterGroup, 2, 4, 4, 2, MIXED, 9, 9, 1>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
+                break;
+            case CLS_Q1_3D_SCALAR:
+                process_mesh<ClusterGroup, 3, 8, 8, 1, MIXED, 4, 0, 1>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
+                break;
+            case CLS_Q1_3D_ELASTIC:
+                process_mesh<ClusterGroup, 3, 8, 8, 3, MIXED, 4, 0, 1>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
+                break;
+            default:
+                process_mesh<ClusterGroup, 2, 9, 4, 1, MIXED, 4, 0, 1>(G, tabs.t[2], s_args, 0, red, xch, &s_flag);
+                break;
+        }
         cl.sync();
         if (cl.block_rank() == 0 && tid == 0) {
             const int slot = __ldcg(&d->slot);
             const long long seq = __ldcg(&d->seq);
-            __threadfence_system();  // u and the stats are visible before the flag
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            ServeTrace tr;
+            tr.t_claim = t_claim;
+            tr.t_end = (long long)gtimer();
+            tr.smid = (int)smid;
+            tr.pad = 0;
+            c.trace[slot] = tr;
+            __threadfence_system();  // u, the stats and the trace are visible before the flag
             st_release_sys(c.done + slot, seq);
         }
     }
@@ -151,7 +253,7 @@ struct Request {
     std::vector<double> X, E, nu, fvals;
     std::vector<int64_t> IEN, ID, fdofs;
     int64_t nN = 0, nEl = 0;
-    int nen = 0;
+    int ndim = 0, fclass = 0, b = 0, nen = 0, plane = 0, cls = 0;
     int64_t need = 0;  // device bytes while in flight
     // in flight
     int slot = -1;
@@ -165,6 +267,7 @@ struct Request {
     int status = SFEM_OK;
     std::vector<double> u;
     sfem_batch_stats stats;
+    ServeTrace trace;
     std::chrono::steady_clock::time_point t_submit, t_publish, t_done;
 };
 
@@ -174,16 +277,16 @@ struct sfem_server {
     sfem_server_config cfg;
     sfem_ctx *ctx = nullptr;               // pattern builds, uploads (ctx->stream)
     cudaStream_t compute = nullptr, copy = nullptr;
-    int nen = 0;
     ServeDesc *ring = nullptr;
     int64_t cap = 0;
-    unsigned long long *head = nullptr;
+    unsigned long long *head = nullptr;  // [0] next descriptor to claim, [1] the kernel's group state
     long long *h_tail = nullptr, *h_done = nullptr;  // mapped host memory: host and device addresses
     int *h_stop = nullptr, *h_exit = nullptr;
     sfem_batch_stats *h_stats = nullptr;
     long long *d_tail = nullptr, *d_done = nullptr;
     int *d_stop = nullptr, *d_exit = nullptr;
     sfem_batch_stats *d_stats = nullptr;
+    ServeTrace *h_trace = nullptr, *d_trace = nullptr;
     std::vector<char> busy;  // ring position in use (descriptor, done flag, stats)
     std::thread worker;
     std::mutex mu;
@@ -202,27 +305,32 @@ struct sfem_server {
 
 namespace {
 
-int64_t request_bytes(const sfem_server *s, int64_t nN, int64_t nEl, int64_t nfix, int64_t nslabs) {
-    const int b = s->cfg.nDof, nen = s->nen;
+int64_t request_bytes(int ndim, int nen, int b, int64_t nN, int64_t nEl, int64_t nfix, int64_t nslabs) {
     const int64_t nd = ((nN + 31) / 32) * 32 * b;
     int64_t bytes = 0;
-    bytes += 8 * (int64_t)s->cfg.ndim * nN;                       // X
+    bytes += 8 * (int64_t)ndim * nN;                              // X
     bytes += 8 * (nEl + 1) + 8 * 2;                               // E, nu
     bytes += 16 * nfix;                                           // fixed dofs + values
     bytes += 8 * (int64_t)sfem_npairs(nen) * b * b * nEl;         // element stiffness
     bytes += (8 + 4) * nslabs * 32 * b * b;                       // K fp64 + fp32
-    bytes += 2 * nd + 8 * 4 * nd + 8 * (5 * nd + nd * b);         // masks, FP64 vectors, CG vectors + minv
+    bytes += 2 * nd + 8 * 4 * nd + 8 * (6 * nd + nd * b);         // masks, FP64 vectors, CG vectors + minv
     bytes += 8 * b * nN;                                          // u
     return bytes;
 }
 
-template <int NDIM, int NEN, int NGP, int B, bool MIXED>
-int launch_serve(sfem_server *s, const ServeCtl &c) {
+// Dynamic shared memory of process_mesh for one class at `threads` per CTA.
+template <int NDIM, int NEN, int NGP>
+size_t class_smem(int threads) {
     constexpr int GS = NEN * NDIM + 1;
-    const int threads = s->cfg.threads;
     const int ngroups = (threads / 32) / NGP;
-    const size_t smem = sizeof(double) * (size_t)ngroups * (NGP * 32 * GS + NGP * 32);
-    auto kern = k_serve<NDIM, NEN, NGP, B, MIXED>;
+    return sizeof(double) * (size_t)ngroups * (NGP * 32 * GS + NGP * 32);
+}
+
+template <bool MIXED>
+int launch_serve(sfem_server *s, const ServeCtl &c) {
+    const int threads = s->cfg.threads;
+    const size_t smem = std::max({class_smem<2, 4, 4>(threads), class_smem<3, 8, 8>(threads), class_smem<2, 9, 4>(threads)});
+    auto kern = k_serve<MIXED>;
     sfem_ctx *ctx = s->ctx;
     SFEM_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     cudaLaunchConfig_t cfg;
@@ -253,18 +361,13 @@ int launch_serve(sfem_server *s, const ServeCtl &c) {
     cfg.gridDim = dim3((unsigned)(groups * csize), 1, 1);
     s->grid = groups * csize;
     s->cluster = csize;
-    const ElemTableB tab = make_table_b(NDIM, s->cfg.function_class);
-    SFEM_CUDA(ctx, cudaLaunchKernelEx(&cfg, kern, tab, c));
+    ServeTables tabs;
+    tabs.t[0] = make_table_b(2, SFEM_Q1);
+    tabs.t[1] = make_table_b(3, SFEM_Q1);
+    tabs.t[2] = make_table_b(2, SFEM_Q2);
+    SFEM_CUDA(ctx, cudaLaunchKernelEx(&cfg, kern, tabs, c));
     SFEM_LAUNCHED(ctx);
     return SFEM_OK;
-}
-
-template <bool MIXED>
-int dispatch_serve(sfem_server *s, const ServeCtl &c) {
-    const int fc = s->cfg.function_class, nd = s->cfg.ndim, b = s->cfg.nDof;
-    if (fc == SFEM_Q2) return launch_serve<2, 9, 4, 1, MIXED>(s, c);
-    if (nd == 2) return b == 1 ? launch_serve<2, 4, 4, 1, MIXED>(s, c) : launch_serve<2, 4, 4, 2, MIXED>(s, c);
-    return b == 1 ? launch_serve<3, 8, 8, 1, MIXED>(s, c) : launch_serve<3, 8, 8, 3, MIXED>(s, c);
 }
 
 int start_kernel(sfem_server *s) {
@@ -277,8 +380,13 @@ int start_kernel(sfem_server *s) {
     c.stop = s->d_stop;
     c.idle_ns = (long long)(s->cfg.idle_exit_ms * 1e6);
     c.exit_reason = s->d_exit;
+    c.trace = s->d_trace;
+    c.state = s->head + 1;
+    // the previous launch has ended (stream order): start with no groups counted
+    if (cudaMemsetAsync(c.state, 0, sizeof(unsigned long long), s->compute) != cudaSuccess)
+        return sfem_set_error(s->ctx, SFEM_CUDA_ERROR, "resetting the serving kernel state");
     *s->h_exit = 0;
-    const int st = s->cfg.solve.precision == SFEM_MIXED ? dispatch_serve<true>(s, c) : dispatch_serve<false>(s, c);
+    const int st = s->cfg.solve.precision == SFEM_MIXED ? launch_serve<true>(s, c) : launch_serve<false>(s, c);
     if (st == SFEM_OK) {
         s->kernel_running = true;
         s->n_launches++;
@@ -301,7 +409,7 @@ void release_request_buffers(sfem_server *s, Request *r) {
 // Place one request on the device and publish it (worker thread, mutex not held).
 int place_request(sfem_server *s, Request *r) {
     sfem_ctx *ctx = s->ctx;
-    const int b = s->cfg.nDof, nd_ = s->cfg.ndim;
+    const int b = r->b, nd_ = r->ndim;
     sfem_mesh *m = nullptr;
     if (r->key != 0) {
         {
@@ -311,7 +419,7 @@ int place_request(sfem_server *s, Request *r) {
         }
         if (!m) {  // first request of this topology: build its pattern (only the worker inserts)
             if (r->IEN.empty()) return sfem_set_error(ctx, SFEM_BAD_ARG, "new topology without IEN");
-            SFEM_TRY(sfem_mesh_create_nel(ctx, nd_, s->cfg.function_class, b, r->nEl, r->X.data(), r->nN,
+            SFEM_TRY(sfem_mesh_create_nel(ctx, nd_, r->fclass, b, r->nEl, r->X.data(), r->nN,
                                           r->IEN.data(), r->nEl, r->nen, b > 1 ? r->ID.data() : nullptr,
                                           SFEM_MEM_HOST, &m));
             int st = sfem_pattern_build(ctx, m, nullptr, nullptr);
@@ -322,14 +430,14 @@ int place_request(sfem_server *s, Request *r) {
             std::lock_guard<std::mutex> lk(s->mu);
             s->topo[r->key].mesh = m;
         }
-        if (m->nN != r->nN || m->nEl != r->nEl)
-            return sfem_set_error(ctx, SFEM_BAD_ARG, "topology key %lld reused with a different mesh size",
+        if (m->nN != r->nN || m->nEl != r->nEl || m->ndim != r->ndim || m->nen != r->nen || m->b != r->b)
+            return sfem_set_error(ctx, SFEM_BAD_ARG, "topology key %lld reused with a different mesh",
                                   (long long)r->key);
         std::lock_guard<std::mutex> lk(s->mu);
         s->topo[r->key].refs++;
         r->mesh = m;
     } else {
-        SFEM_TRY(sfem_mesh_create_nel(ctx, nd_, s->cfg.function_class, b, r->nEl, r->X.data(), r->nN, r->IEN.data(),
+        SFEM_TRY(sfem_mesh_create_nel(ctx, nd_, r->fclass, b, r->nEl, r->X.data(), r->nN, r->IEN.data(),
                                       r->nEl, r->nen, b > 1 ? r->ID.data() : nullptr, SFEM_MEM_HOST, &m));
         r->mesh = m;  // released with the request
         SFEM_TRY(sfem_pattern_build(ctx, m, nullptr, nullptr));
@@ -364,7 +472,7 @@ int place_request(sfem_server *s, Request *r) {
     SFEM_TRY(alloc((void **)&b64, sizeof(double) * ndp, "request rhs"));
     SFEM_TRY(alloc((void **)&x64, sizeof(double) * ndp, "request x"));
     SFEM_TRY(alloc((void **)&q64, sizeof(double) * ndp, "request q"));
-    SFEM_TRY(alloc(&vecT, sizeof(double) * (5 * ndp + ndp * b), "request CG vectors"));
+    SFEM_TRY(alloc(&vecT, sizeof(double) * (6 * ndp + ndp * b), "request CG vectors"));
     SFEM_TRY(alloc((void **)&u, sizeof(double) * (b * nN + 1), "request u"));
     SFEM_TRY(sfem_copy_in(ctx, X, r->X.data(), sizeof(double) * nd_ * nN, SFEM_MEM_HOST));
     SFEM_TRY(sfem_copy_in(ctx, E, r->E.data(), sizeof(double) * r->E.size(), SFEM_MEM_HOST));
@@ -407,7 +515,7 @@ int place_request(sfem_server *s, Request *r) {
     a.nE = (int64_t)r->E.size();
     a.nu = NU;
     a.nNu = (int64_t)r->nu.size();
-    a.plane = s->cfg.plane;
+    a.plane = r->plane;
     a.fix_dofs = fd;
     a.fix_vals = fv;
     a.kbuf = kbuf;
@@ -431,6 +539,7 @@ int place_request(sfem_server *s, Request *r) {
     a.err = ctx->d_err;
     d.seq = r->seq;
     d.slot = slot;
+    d.cls = r->cls;
     SFEM_CUDA(ctx, cudaMemcpyAsync(&s->ring[slot], &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
     SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SFEM_OK;
@@ -514,6 +623,7 @@ void worker_loop(sfem_server *s) {
             cudaStreamSynchronize(s->copy);
             lk.lock();
             r->stats = s->h_stats[r->slot];
+            r->trace = s->h_trace[r->slot];
             r->status = r->stats.status;
             release_request_buffers(s, r);
             s->bytes_in_use -= r->need;
@@ -548,10 +658,6 @@ void worker_loop(sfem_server *s) {
 extern "C" void sfem_server_config_default(sfem_server_config *c) {
     if (!c) return;
     memset(c, 0, sizeof(*c));
-    c->ndim = 3;
-    c->function_class = SFEM_Q1;
-    c->nDof = 3;
-    c->plane = SFEM_PLANE_STRESS;
     c->cluster = 4;
     c->threads = 512;
     c->sm_fraction = 0.9;  // leave SMs for the pattern builds of new topologies
@@ -571,15 +677,11 @@ extern "C" int sfem_server_create(int device, const sfem_server_config *cfg, sfe
     sfem_server_config c;
     sfem_server_config_default(&c);
     if (cfg) c = *cfg;
-    if ((c.ndim != 2 && c.ndim != 3) || (c.nDof != 1 && c.nDof != c.ndim) ||
-        (c.function_class != SFEM_Q1 && c.function_class != SFEM_Q2) ||
-        (c.function_class == SFEM_Q2 && (c.ndim != 2 || c.nDof != 1)) ||
-        (c.cluster != 1 && c.cluster != 2 && c.cluster != 4 && c.cluster != 8) ||
+    if ((c.cluster != 1 && c.cluster != 2 && c.cluster != 4 && c.cluster != 8) ||
         (c.threads != 256 && c.threads != 512) || c.max_inflight < 1 || !(c.idle_exit_ms > 0.0))
         return SFEM_BAD_ARG;
     sfem_server *s = new sfem_server();
     s->cfg = c;
-    s->nen = c.function_class == SFEM_Q2 ? 9 : (1 << c.ndim);
     int st = sfem_ctx_create(device, &s->ctx);
     if (st != SFEM_OK) {
         delete s;
@@ -592,8 +694,8 @@ extern "C" int sfem_server_create(int device, const sfem_server_config *cfg, sfe
         if ((st = sfem_cuda_status(ctx, cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking), "stream"))) break;
         s->cap = c.max_inflight;
         if ((st = sfem_cuda_status(ctx, cudaMalloc(&s->ring, sizeof(ServeDesc) * s->cap), "ring"))) break;
-        if ((st = sfem_cuda_status(ctx, cudaMalloc(&s->head, sizeof(unsigned long long)), "head"))) break;
-        if ((st = sfem_cuda_status(ctx, cudaMemset(s->head, 0, sizeof(unsigned long long)), "head"))) break;
+        if ((st = sfem_cuda_status(ctx, cudaMalloc(&s->head, 2 * sizeof(unsigned long long)), "head"))) break;
+        if ((st = sfem_cuda_status(ctx, cudaMemset(s->head, 0, 2 * sizeof(unsigned long long)), "head"))) break;
         if ((st = sfem_cuda_status(ctx, cudaHostAlloc((void **)&s->h_tail, 64, cudaHostAllocMapped), "tail"))) break;
         if ((st = sfem_cuda_status(ctx, cudaHostAlloc((void **)&s->h_stop, 64, cudaHostAllocMapped), "stop"))) break;
         if ((st = sfem_cuda_status(ctx, cudaHostAlloc((void **)&s->h_exit, 64, cudaHostAllocMapped), "exit"))) break;
@@ -603,7 +705,11 @@ extern "C" int sfem_server_create(int device, const sfem_server_config *cfg, sfe
         if ((st = sfem_cuda_status(ctx, cudaHostAlloc((void **)&s->h_stats, sizeof(sfem_batch_stats) * s->cap,
                                                       cudaHostAllocMapped), "stats")))
             break;
-        if ((st = sfem_cuda_status(ctx, cudaHostGetDevicePointer((void **)&s->d_tail, s->h_tail, 0), "tail")) ||
+        if ((st = sfem_cuda_status(ctx, cudaHostAlloc((void **)&s->h_trace, sizeof(ServeTrace) * s->cap,
+                                                      cudaHostAllocMapped), "trace")))
+            break;
+        if ((st = sfem_cuda_status(ctx, cudaHostGetDevicePointer((void **)&s->d_trace, s->h_trace, 0), "trace")) ||
+            (st = sfem_cuda_status(ctx, cudaHostGetDevicePointer((void **)&s->d_tail, s->h_tail, 0), "tail")) ||
             (st = sfem_cuda_status(ctx, cudaHostGetDevicePointer((void **)&s->d_stop, s->h_stop, 0), "stop")) ||
             (st = sfem_cuda_status(ctx, cudaHostGetDevicePointer((void **)&s->d_exit, s->h_exit, 0), "exit")) ||
             (st = sfem_cuda_status(ctx, cudaHostGetDevicePointer((void **)&s->d_done, s->h_done, 0), "done")) ||
@@ -627,20 +733,28 @@ extern "C" int sfem_server_create(int device, const sfem_server_config *cfg, sfe
     return SFEM_OK;
 }
 
-extern "C" int sfem_server_submit(sfem_server *s, int64_t topology_key, const double *NodeList, int64_t nNodes,
-                                  const int64_t *IEN, int64_t nEl, int nen, const int64_t *ID, const double *Young,
-                                  int64_t nYoung, const double *nu, int64_t nNu, const int64_t *fixed_dofs,
-                                  int64_t nfix, const double *fixed_vals, int64_t *request_id) {
-    if (!s || !request_id || !NodeList || nNodes < 1 || nEl < 1 || nen != s->nen || nfix < 0) return SFEM_BAD_ARG;
-    const int b = s->cfg.nDof;
+extern "C" int sfem_server_submit(sfem_server *s, int ndim, int function_class, int nDof, int plane,
+                                  int64_t topology_key, const double *NodeList, int64_t nNodes, const int64_t *IEN,
+                                  int64_t nEl, const int64_t *ID, const double *Young, int64_t nYoung,
+                                  const double *nu, int64_t nNu, const int64_t *fixed_dofs, int64_t nfix,
+                                  const double *fixed_vals, int64_t *request_id) {
+    if (!s || !request_id || !NodeList || nNodes < 1 || nEl < 1 || nfix < 0) return SFEM_BAD_ARG;
+    const int cls = serve_class(ndim, function_class, nDof);
+    if (cls < 0 || (plane != SFEM_PLANE_STRESS && plane != SFEM_PLANE_STRAIN)) return SFEM_BAD_ARG;
+    const int b = nDof, nen = function_class == SFEM_Q2 ? 9 : (1 << ndim);
     if (b > 1 && (!Young || !nu || (nYoung != 1 && nYoung != nEl) || nNu != 1)) return SFEM_BAD_ARG;
     if (nfix > 0 && (!fixed_dofs || !fixed_vals)) return SFEM_BAD_ARG;
     Request *r = new Request();
     r->key = topology_key;
     r->nN = nNodes;
     r->nEl = nEl;
+    r->ndim = ndim;
+    r->fclass = function_class;
+    r->b = b;
     r->nen = nen;
-    r->X.assign(NodeList, NodeList + s->cfg.ndim * nNodes);
+    r->plane = plane;
+    r->cls = cls;
+    r->X.assign(NodeList, NodeList + (int64_t)ndim * nNodes);
     bool cached;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -664,9 +778,9 @@ extern "C" int sfem_server_submit(sfem_server *s, int64_t topology_key, const do
     }
     r->fdofs.assign(fixed_dofs, fixed_dofs + nfix);
     r->fvals.assign(fixed_vals, fixed_vals + nfix);
-    // footprint estimate from the structured-neighbour bound (27 / 9 node blocks per row)
-    const int64_t width = s->cfg.ndim == 3 ? 27 : (s->nen == 9 ? 25 : 9);
-    r->need = request_bytes(s, nNodes, nEl, nfix, ((nNodes + 31) / 32) * width);
+    // footprint estimate from the structured-neighbour bound (27 / 25 / 9 node blocks per row)
+    const int64_t width = ndim == 3 ? 27 : (nen == 9 ? 25 : 9);
+    r->need = request_bytes(ndim, nen, b, nNodes, nEl, nfix, ((nNodes + 31) / 32) * width);
     r->t_submit = std::chrono::steady_clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
     if (topology_key != 0 && !cached) s->topo[topology_key];  // placed (pattern built) in submission order
@@ -701,6 +815,9 @@ extern "C" int sfem_server_wait(sfem_server *s, int64_t request_id, double timeo
         res->queue_ms = std::chrono::duration<double, std::milli>(r->t_publish - r->t_submit).count();
         res->total_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
         res->ndof = r->ndof;
+        res->t_claim_ms = r->trace.t_claim * 1e-6;
+        res->t_end_ms = r->trace.t_end * 1e-6;
+        res->smid = r->trace.smid;
     }
     if (u_out && u_len > 0) memcpy(u_out, r->u.data(), sizeof(double) * std::min<int64_t>(u_len, (int64_t)r->u.size()));
     s->requests.erase(it);
@@ -757,6 +874,7 @@ extern "C" int sfem_server_destroy(sfem_server *s) {
     if (s->h_exit) cudaFreeHost(s->h_exit);
     if (s->h_done) cudaFreeHost(s->h_done);
     if (s->h_stats) cudaFreeHost(s->h_stats);
+    if (s->h_trace) cudaFreeHost(s->h_trace);
     if (s->compute) cudaStreamDestroy(s->compute);
     if (s->copy) cudaStreamDestroy(s->copy);
     if (s->ctx) sfem_ctx_destroy(s->ctx);

@@ -430,23 +430,19 @@ class Batch:
 
 
 class Server:
-    """A device-resident request loop for one element class (sfem_server_*).
+    """A device-resident request loop (sfem_server_*).
 
     ``submit`` queues one mesh (reference shapes, 1-based indices, host
     arrays) and returns a request id at once; ``wait`` returns its
-    displacements.  A persistent kernel takes requests as they arrive and
-    solves many at once; requests sharing a ``topology_key`` reuse the
-    sparsity pattern built for the first of them.
+    displacements.  One persistent kernel takes requests of any element
+    class as they arrive and solves many at once; requests sharing a
+    ``topology_key`` reuse the sparsity pattern built for the first of them.
     """
 
-    def __init__(self, ndim=3, nDof=3, FunctionClass="Q1", plane="stress", cluster=4, threads=512,
-                 sm_fraction=0.9, hbm_budget_fraction=0.5, hbm_budget_bytes=0, max_inflight=1024,
-                 idle_exit_ms=20.0, device=0, **solve_kw):
+    def __init__(self, cluster=4, threads=512, sm_fraction=0.9, hbm_budget_fraction=0.5,
+                 hbm_budget_bytes=0, max_inflight=1024, idle_exit_ms=20.0, device=0, **solve_kw):
         cfg = L.ServerConfig()
         lib().sfem_server_config_default(C.byref(cfg))
-        cfg.ndim, cfg.nDof = int(ndim), int(nDof)
-        cfg.function_class = {"Q1": L.Q1, "Q2": L.Q2}[FunctionClass]
-        cfg.plane = _plane(plane)
         cfg.cluster, cfg.threads = int(cluster), int(threads)
         cfg.sm_fraction = float(sm_fraction)
         cfg.hbm_budget_fraction = float(hbm_budget_fraction)
@@ -456,8 +452,6 @@ class Server:
         kw = {"precision": "mixed", "precond": "block_jacobi", "rtol": 1e-8}
         kw.update(solve_kw)
         cfg.solve = _solve_opts(**kw)
-        self.ndim, self.nDof = cfg.ndim, cfg.nDof
-        self.nen = 9 if FunctionClass == "Q2" else 2 ** cfg.ndim
         h = C.c_void_p()
         check(lib().sfem_server_create(int(device), C.byref(cfg), C.byref(h)))
         self.h = h
@@ -465,7 +459,11 @@ class Server:
         self._nel_of_key = {}
 
     def submit(self, NodeList, IEN=None, ID=None, Young=1.0, nu=0.3, fixed_dofs=(), fixed_vals=(),
-               topology_key=0):
+               topology_key=0, ndim=None, nDof=None, FunctionClass="Q1", plane="stress"):
+        """``ndim`` defaults to the rows of ``NodeList``; ``nDof`` to ``ndim``
+        when ``ID`` is given (elasticity), else 1."""
+        ndim = int(ndim if ndim is not None else np.shape(NodeList)[0])
+        nDof = int(nDof if nDof is not None else (ndim if ID is not None else 1))
         X = _Buf(NodeList, np.float64)
         E = np.ascontiguousarray(np.atleast_1d(np.asarray(Young, dtype=np.float64)).ravel())
         V = np.ascontiguousarray(np.atleast_1d(np.asarray(nu, dtype=np.float64)).ravel())
@@ -477,19 +475,20 @@ class Server:
         nEl = np.shape(IEN)[0] if IEN is not None else self._nel_of_key.get(topology_key)
         if nEl is None:
             raise SfemError(L.SFEM_BAD_ARG, "IEN is needed for a topology key not submitted before")
-        Ib, Db = _Buf(IEN, np.int64), _Buf(ID if self.nDof > 1 else None, np.int64)
+        Ib, Db = _Buf(IEN, np.int64), _Buf(ID if nDof > 1 else None, np.int64)
         if X.space != L.MEM_HOST or Ib.space != L.MEM_HOST:
             raise SfemError(L.SFEM_BAD_ARG, "server requests are host arrays")
+        fc = {"Q1": L.Q1, "Q2": L.Q2}[FunctionClass]
         rid = C.c_int64()
-        code = lib().sfem_server_submit(self.h, int(topology_key), X.ptr, nN, Ib.ptr, nEl, self.nen,
-                                        Db.ptr, E.ctypes.data, E.size, V.ctypes.data, V.size,
-                                        fd.ctypes.data if fd.size else None, fd.size,
+        code = lib().sfem_server_submit(self.h, ndim, fc, nDof, _plane(plane), int(topology_key), X.ptr,
+                                        nN, Ib.ptr, nEl, Db.ptr, E.ctypes.data, E.size, V.ctypes.data,
+                                        V.size, fd.ctypes.data if fd.size else None, fd.size,
                                         fv.ctypes.data if fv.size else None, C.byref(rid))
         if code:
             raise SfemError(code, "sfem_server_submit")
         if topology_key and IEN is not None:
             self._nel_of_key[topology_key] = nEl
-        self._ndof[rid.value] = self.nDof * nN
+        self._ndof[rid.value] = nDof * nN
         return rid.value
 
     def wait(self, request_id, timeout_ms=-1.0):

@@ -88,9 +88,9 @@ def test_no_gpu_fails_loudly(sfem):
     with pytest.raises(sfem.SfemError):
         sfem.Context(0)
     with pytest.raises(sfem.SfemError):
-        sfem.Server(ndim=2, nDof=2)
+        sfem.Server()
     with pytest.raises(KeyError):
-        sfem.Server(ndim=2, nDof=2, precision="fp16")
+        sfem.Server(precision="fp16")
 
 
 def test_missing_library_is_an_error(sfem, monkeypatch, tmp_path):

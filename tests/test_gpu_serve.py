@@ -37,11 +37,12 @@ def _single(sfem, ctx, p, rtol=1e-13):
 
 def _submit(srv, p, key=0, with_ien=True):
     return srv.submit(p.NodeList, p.IEN[: p.n_elem] if with_ien else None, p.ID if with_ien else None,
-                      p.Young, p.nu, p.fixed_dofs, p.fixed_vals, topology_key=key)
+                      p.Young, p.nu, p.fixed_dofs, p.fixed_vals, topology_key=key, ndim=p.ndim,
+                      nDof=p.ndim, plane=p.plane)
 
 
-def _server2d(sfem, **kw):
-    args = dict(ndim=2, nDof=2, plane="strain", cluster=4, rtol=1e-12, idle_exit_ms=50.0)
+def _server(sfem, **kw):
+    args = dict(cluster=4, rtol=1e-12, idle_exit_ms=50.0)
     args.update(kw)
     return sfem.Server(**args)
 
@@ -49,7 +50,7 @@ def _server2d(sfem, **kw):
 @pytest.mark.timeout(300)
 def test_served_requests_match_single_mesh_solves(sfem, ctx):
     probs = _quads([5, 17, 9, 33, 2, 24, 12, 40, 3, 61], e_sigma=0.5)
-    with _server2d(sfem) as srv:
+    with _server(sfem) as srv:
         ids = [_submit(srv, p) for p in probs]
         for p, rid in zip(probs, ids):
             u, res = srv.wait(rid, timeout_ms=60000)
@@ -67,7 +68,7 @@ def test_same_alone_and_in_the_mix(sfem, ctx, precision):
     """A request's displacements are bitwise identical served alone and
     served while other requests share the GPU."""
     probs = _quads([30, 7, 19, 26, 11, 44], seed=21)
-    with _server2d(sfem, precision=precision) as srv:
+    with _server(sfem, precision=precision) as srv:
         alone = {}
         for k in (0, 3, 5):
             alone[k], _ = srv.wait(_submit(srv, probs[k]), timeout_ms=60000)
@@ -75,7 +76,7 @@ def test_same_alone_and_in_the_mix(sfem, ctx, precision):
         mixed = [srv.wait(i, timeout_ms=60000)[0] for i in ids]
     for k, u in alone.items():
         assert np.array_equal(u, mixed[k])
-    with _server2d(sfem, precision=precision) as srv2:   # another server, reversed order
+    with _server(sfem, precision=precision) as srv2:   # another server, reversed order
         ids = [_submit(srv2, p) for p in probs[::-1]]
         rev = [srv2.wait(i, timeout_ms=60000)[0] for i in ids][::-1]
     for a, b in zip(rev, mixed):
@@ -86,7 +87,7 @@ def test_same_alone_and_in_the_mix(sfem, ctx, precision):
 def test_admission_by_hbm_budget(sfem, ctx):
     """With a budget below one request's footprint, requests still run, one at a time."""
     probs = _quads([12, 20, 8, 16], seed=5)
-    with _server2d(sfem, hbm_budget_bytes=1) as srv:
+    with _server(sfem, hbm_budget_bytes=1) as srv:
         ids = [_submit(srv, p) for p in probs]
         outs = [srv.wait(i, timeout_ms=60000) for i in ids]
         info = srv.info()
@@ -102,7 +103,7 @@ def test_topology_cache(sfem, ctx):
     mg = sfem.meshgen
     probs = [mg.quad_problem(14, 100 + k, jitter=0.15, nu_range=(0.2, 0.45), e_sigma=0.3,
                              plane="strain") for k in range(5)]
-    with _server2d(sfem) as srv:
+    with _server(sfem) as srv:
         ids = [_submit(srv, p, key=14, with_ien=(k == 0)) for k, p in enumerate(probs)]
         outs = [srv.wait(i, timeout_ms=60000) for i in ids]
         assert srv.info()["topologies"] == 1
@@ -114,7 +115,7 @@ def test_topology_cache(sfem, ctx):
 @pytest.mark.timeout(300)
 def test_idle_exit_and_relaunch(sfem, ctx):
     probs = _quads([9, 13], seed=8)
-    with _server2d(sfem, idle_exit_ms=5.0) as srv:
+    with _server(sfem, idle_exit_ms=5.0) as srv:
         u0, r0 = srv.wait(_submit(srv, probs[0]), timeout_ms=60000)
         time.sleep(0.3)                                   # the kernel leaves after 5 ms idle
         u1, r1 = srv.wait(_submit(srv, probs[1]), timeout_ms=60000)
@@ -127,7 +128,7 @@ def test_idle_exit_and_relaunch(sfem, ctx):
 def test_3d_hex_and_scalar_requests(sfem, ctx):
     mg = sfem.meshgen
     probs = [mg.hex_problem(n, 40 + n, jitter=0.2, e_sigma=0.5, nu=0.3, top="modes") for n in (3, 7, 5)]
-    with sfem.Server(ndim=3, nDof=3, cluster=2, rtol=1e-12) as srv:
+    with sfem.Server(cluster=2, rtol=1e-12) as srv:
         ids = [_submit(srv, p) for p in probs]
         for p, i in zip(probs, ids):
             u, res = srv.wait(i, timeout_ms=60000)
@@ -139,24 +140,44 @@ def test_3d_hex_and_scalar_requests(sfem, ctx):
     K = sfem.assemble_system(11, NL, IEN, 2, "Q1", 1, ctx=ctx, as_handle=True)
     ref = K.solve(bnd, v, rtol=1e-13)[0]
     K.close()
-    with sfem.Server(ndim=2, nDof=1, cluster=1, rtol=1e-12) as srv:
+    with sfem.Server(cluster=1, rtol=1e-12) as srv:
         u, res = srv.wait(srv.submit(NL, IEN, None, 1.0, 0.3, bnd, v), timeout_ms=60000)
     assert res["status"] == 0 and _rel(u, ref) <= TOL_U
 
 
 @pytest.mark.timeout(300)
+def test_mixed_classes_in_one_stream(sfem, ctx):
+    """2D and 3D requests interleaved on one server, each matching its own solve."""
+    mg = sfem.meshgen
+    probs = []
+    for k, n in enumerate((6, 4, 21, 5, 13, 3)):
+        if k % 2:
+            probs.append(mg.hex_problem(n, 90 + n, jitter=0.2, e_sigma=0.5, nu=0.3, top="modes"))
+        else:
+            probs.append(_quads([n], seed=60 + n, e_sigma=0.4)[0])
+    with _server(sfem) as srv:
+        ids = [_submit(srv, p) for p in probs]
+        outs = [srv.wait(i, timeout_ms=60000) for i in ids]
+    for p, (u, res) in zip(probs, outs):
+        assert res["status"] == 0
+        assert _rel(u, _single(sfem, ctx, p)) <= TOL_U, p.name
+
+
+@pytest.mark.timeout(300)
 def test_errors_and_shutdown_with_work_outstanding(sfem, ctx):
     probs = _quads([6, 10], seed=2)
-    with _server2d(sfem) as srv:
+    with _server(sfem) as srv:
         bad = srv.submit(probs[0].NodeList, probs[0].IEN, probs[0].ID, 1.0, 0.3,
-                         np.array([10 ** 6]), np.zeros(1))
+                         np.array([10 ** 6]), np.zeros(1), plane="strain")
         good = _submit(srv, probs[1])
         _, rb = srv.wait(bad, timeout_ms=60000)
         ug, rg = srv.wait(good, timeout_ms=60000)
         assert rb["status"] == 2 and rg["status"] == 0      # the bad request alone fails
         with pytest.raises(sfem.SfemError):
             srv.submit(probs[0].NodeList, None, None, 1.0, 0.3, [], [], topology_key=77)
-    srv = _server2d(sfem)
+        with pytest.raises(sfem.SfemError):                  # elasticity with nDof 3 in 2D
+            srv.submit(probs[0].NodeList, probs[0].IEN, probs[0].ID, 1.0, 0.3, [], [], nDof=3)
+    srv = _server(sfem)
     for _ in range(3):
         for p in _quads([40, 50, 60], seed=4):
             _submit(srv, p)
