@@ -294,6 +294,37 @@ SFEM_API int sfem_batch_get_launch(const sfem_batch *batch, int *threads, int *c
                                    int *cluster, int64_t *cluster_min_nodes, int *last_grid);
 SFEM_API int sfem_batch_destroy(sfem_batch *batch);
 
+/* ---- load increments ------------------------------------------------------ */
+
+/* The driver's load-increment loop (examples/vector3D.jl:310-338): one K,
+ * one set of prescribed DOFs, nsteps sets of prescribed values -- step s
+ * reads fixed_vals[s*nfix .. s*nfix+nfix) and writes u_out[s*n .. s*n+n),
+ * n = the matrix size; stats (optional) has nsteps entries.  No single
+ * reference counterpart (the reference re-inverts K_free at every step).
+ * warm_start != 0 starts step s from the affine combination of up to three
+ * earlier solutions whose prescribed values best match step s's: the
+ * solution is affine in the prescribed values, so on the reference's
+ * linear load path (q_d = -d on the top face) every step after the second
+ * starts at the answer and needs no CG iteration. */
+SFEM_API int sfem_solve_increments(sfem_ctx *ctx, sfem_matrix *K, const int64_t *fixed_dofs, int64_t nfix,
+                                   const double *fixed_vals, int64_t nsteps, const double *f, double *u_out,
+                                   int mem_space, const sfem_solve_opts *opts, int warm_start,
+                                   sfem_solve_stats *stats);
+
+/* ---- surface penalty ------------------------------------------------------ */
+
+/* K <- K + beta * b in place, where b is the surface penalty ("slip") matrix
+ * of apply_boundary_conditions (examples/vector3D.jl:175-264) and the sum is
+ * the driver's K_bar = K + beta*b (examples/vector3D.jl:306-308).  3D Q1
+ * elasticity only (the reference's 2D branch cannot run).  NodeList: the
+ * 3 x nNodes coordinates the faces are integrated on (the reference passes
+ * the inflated cylinder, not K's cube); IEN_faces: nFaces x 4, column-major,
+ * 1-based -- the reference's order is [IEN_btm; IEN_top].  Every face node
+ * pair must already be coupled in K (true for faces of K's elements).  The
+ * FP32 copies used by the mixed solver are refreshed. */
+SFEM_API int sfem_penalty_add(sfem_ctx *ctx, sfem_matrix *K, const double *NodeList, const int64_t *IEN_faces,
+                              int64_t nFaces, int nenFace, double beta, int mem_space);
+
 /* ---- serving: a device-resident request loop ------------------------------ */
 
 /* A server runs one persistent kernel that takes assemble-and-solve requests

@@ -19,6 +19,10 @@ What it restates (reference paths are relative to the smearFEM.jl project):
   set_boundary_cond       examples/vector3D.jl:133-173
   solve_eliminated        examples/vector3D.jl:315-322 (dense ``inv`` of
                           ``K_free = C' K C``, ``q = q_d + C q_f``)
+  apply_boundary_conditions_loops
+                          examples/vector3D.jl:175-264 (surface penalty b)
+  add_scaled              examples/vector3D.jl:308 (K_bar = K + beta*b)
+  inflate_sphere          src/PostProcess.jl:30-44
 
 Parity pinning.  ``gaussian_quadrature`` and ``basis_function`` are pinned by
 the reference's own known-answer tests (test/runtests.jl:15-35; restated in
@@ -564,3 +568,105 @@ def solve_eliminated(K_csc, fixed_dofs, fixed_vals, f=None, method="inv"):
     q = q_d.copy()
     q[free] += qf
     return q
+
+
+# --------------------------------------------------------------------------
+# examples/vector3D.jl:175-264 (surface penalty), :306-308 (K_bar = K + beta b)
+# and src/PostProcess.jl:30-44 (inflate_sphere)
+# --------------------------------------------------------------------------
+
+
+def apply_boundary_conditions_loops(ne, NodeList, IEN, IEN_top, IEN_btm, ndim, FunctionClass="Q1",
+                                    ID=None, nDof=3):
+    """Line-by-line restatement of ``apply_boundary_conditions``
+    (examples/vector3D.jl:175-264): the penalty ("slip") matrix ``b`` of the
+    top and bottom surfaces, b = sum over surface quads and their 2x2 Gauss
+    points of w |dx/dxi x dx/deta| M'M with M = [N_1 I, ..., N_4 I] (3 x 12).
+
+    COO layout as the reference: bottom faces first (inz_btm), then top faces
+    (inz_top), each face a 4x4 grid of 3x3 blocks (iNode, jNode, iDof, jDof);
+    ``V[inz] +=`` per Gauss point; then ``sparse``.  Only 3D exists: the 2D
+    branch takes ``cross`` of 2-vectors, which the reference cannot evaluate.
+    ``IEN`` is unused, as in the reference.
+    """
+    if ndim != 3:
+        raise ValueError("apply_boundary_conditions: the reference's 2D branch calls cross() on "
+                         "2-vectors (examples/vector3D.jl:218), so only ndim = 3 is defined")
+    NodeList = np.asarray(NodeList, dtype=np.float64)
+    IEN_top = np.asarray(IEN_top, dtype=np.int64)
+    IEN_btm = np.asarray(IEN_btm, dtype=np.int64)
+    ID = np.asarray(ID, dtype=np.int64)
+    nface = int(ne) ** (ndim - 1)
+    if min(IEN_top[:nface].min(), IEN_btm[:nface].min()) < 1:
+        raise IndexError("surface connectivity holds node 0 (the reference's meshgrid leaves "
+                         "IEN_top empty when ne = 1)")
+    L = nface * (ID.shape[1] * IEN_btm.shape[1]) ** 2 * 2
+    E = np.zeros(L, np.int64)
+    J = np.zeros(L, np.int64)
+    V = np.zeros(L, np.float64)
+    xi, w_xi = gaussian_quadrature(-1, 1)
+    eta, w_eta = gaussian_quadrature(-1, 1)
+    wpoints = [w_xi[0] * w_eta[0], w_xi[1] * w_eta[0], w_xi[1] * w_eta[1], w_xi[0] * w_eta[1]]
+    x = [xi[0], xi[1], xi[1], xi[0]]
+    y = [eta[0], eta[0], eta[1], eta[1]]
+    for e in range(nface):
+        coords_top = NodeList[:, IEN_top[e, :] - 1]
+        coords_btm = NodeList[:, IEN_btm[e, :] - 1]
+        for gp in range(2 ** (ndim - 1)):
+            N, dN = basis_function(x[gp], y[gp], None, FunctionClass)
+            dx_top = coords_top @ dN
+            dx_btm = coords_btm @ dN
+            w_top = wpoints[gp] * np.linalg.norm(np.cross(dx_top[:, 0], dx_top[:, 1]))
+            w_btm = wpoints[gp] * np.linalg.norm(np.cross(dx_btm[:, 0], dx_btm[:, 1]))
+            M = np.zeros((3, ndim * N.shape[0]))
+            M[0, 0::nDof] = N
+            M[1, 1::nDof] = N
+            M[2, 2::nDof] = N
+            be = M.T @ M
+            nb = be.shape[0]
+            for iNode in range(nb // nDof):
+                for jNode in range(nb // nDof):
+                    for iDof in range(ID.shape[1]):
+                        for jDof in range(ID.shape[1]):
+                            i = iNode * nDof + iDof
+                            j = jNode * nDof + jDof
+                            inz_btm = (be.size * e + iNode * nDof * nb + jNode * nDof ** 2
+                                       + iDof * nDof + jDof)
+                            inz_top = be.size * nface + inz_btm
+                            E[inz_top] = ID[IEN_top[e, iNode] - 1, iDof]
+                            J[inz_top] = ID[IEN_top[e, jNode] - 1, jDof]
+                            V[inz_top] += w_top * be[i, j]
+                            E[inz_btm] = ID[IEN_btm[e, iNode] - 1, iDof]
+                            J[inz_btm] = ID[IEN_btm[e, jNode] - 1, jDof]
+                            V[inz_btm] += w_btm * be[i, j]
+    return julia_sparse(E, J, V)
+
+
+def add_scaled(K_csc, beta, b_csc):
+    """``K + beta * b`` for two CSC matrices (examples/vector3D.jl:308) as a
+    scipy CSC matrix: each stored entry of ``beta * b`` is rounded once, then
+    added to K's entry."""
+    K = csc_to_scipy(*K_csc)
+    b = csc_to_scipy(*b_csc)
+    b.data = beta * b.data
+    if b.shape != K.shape:
+        b.resize(K.shape)
+    return (K + b).tocsc()
+
+
+def inflate_sphere(NodeList, x0, x1, y0, y1):
+    """``inflate_sphere`` (src/PostProcess.jl:30-44) on a copy: every node's
+    (x, y) is moved radially so that the square cross-section becomes a disc
+    (scale = max(|dx|, |dy|) about the centre, new radius = scale).  The
+    reference mutates its argument; this returns a new array."""
+    out = np.array(NodeList, dtype=np.float64, copy=True)
+    xc = np.array([0.5 * (x0 + x1), 0.5 * (y0 + y1)])
+    for i in range(out.shape[1]):
+        d = out[0:2, i] - xc
+        scale = np.max(np.abs(d))
+        if scale == 0.0:  # Julia's `scale ≈ 0.` (rtol sqrt(eps), atol 0) holds only for exact 0
+            out[0:2, i] = [0.0, 0.0]
+        else:
+            r = math.sqrt((out[0, i] - xc[0]) ** 2 + (out[1, i] - xc[1]) ** 2)
+            out[0:2, i] = scale * (out[0:2, i] - xc) / r
+    return out

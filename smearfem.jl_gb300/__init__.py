@@ -6,6 +6,7 @@ include/smearfem_gpu.h); this package is the host-side mirror of the
 reference's Julia calling surface plus the seeded mesh generators.
 """
 from ._lib import SfemError, lib  # noqa: F401
-from .fem import (Batch, Context, Matrix, Mesh, Server, assemble_system, basis_function,  # noqa: F401
-                  gaussian_quadrature, get_context, solve_dirichlet, version)
+from .fem import (Batch, Context, Matrix, Mesh, Server, apply_boundary_conditions,  # noqa: F401
+                  assemble_system, basis_function, gaussian_quadrature, get_context,
+                  solve_dirichlet, version)
 from . import meshgen  # noqa: F401

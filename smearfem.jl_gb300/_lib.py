@@ -117,6 +117,9 @@ SIGNATURES = {
     "sfem_batch_destroy": (C.c_int, [P]),
     "sfem_solve_dirichlet": (C.c_int, [P, P, P, I64, P, P, P, C.c_int, C.POINTER(SolveOpts),
                                        C.POINTER(SolveStats)]),
+    "sfem_penalty_add": (C.c_int, [P, P, P, P, I64, C.c_int, C.c_double, C.c_int]),
+    "sfem_solve_increments": (C.c_int, [P, P, P, I64, P, I64, P, P, C.c_int, C.POINTER(SolveOpts), C.c_int,
+                                        P]),
     "sfem_server_config_default": (None, [C.POINTER(ServerConfig)]),
     "sfem_server_create": (C.c_int, [C.c_int, C.POINTER(ServerConfig), PP]),
     "sfem_server_submit": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, I64, P, I64, P, I64, P,

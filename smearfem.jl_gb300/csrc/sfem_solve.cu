@@ -366,6 +366,11 @@ __global__ void k_gather_global(const double *__restrict__ fg, int64_t n, const 
     if (i >= 0) fi[i] = fg[g];
 }
 
+__global__ void k_zero_fixed(int64_t nd, const unsigned char *__restrict__ fixed, double *__restrict__ x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nd && fixed[i]) x[i] = 0.0;
+}
+
 // b = f - K ud on free DOFs (0 on fixed).
 __global__ void k_rhs(int64_t nd, const double *__restrict__ f, const double *__restrict__ Kud,
                       const unsigned char *__restrict__ fixed, double *__restrict__ bvec) {
@@ -619,8 +624,10 @@ class Solver {
         cudaStreamSynchronize(ctx->stream);
     }
 
+    // u0: optional initial guess in global DOF numbering (its prescribed
+    // entries are ignored); NULL starts from zero.
     int run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_vals, const double *f, double *u_out,
-            int mem_space, sfem_solve_stats *stats);
+            int mem_space, sfem_solve_stats *stats, const double *u0 = nullptr);
 
    private:
     template <typename T>
@@ -644,6 +651,7 @@ class Solver {
     std::vector<void *> owned;
     unsigned char *fixed = nullptr, *gfixed = nullptr;
     double *ud = nullptr, *bvec = nullptr, *partial = nullptr;
+    double *r0vec = nullptr;  // initial residual: bvec, or b - K x0 for a warm start
     CgScalars *S = nullptr;
     int64_t nd = 0;  // internal DOFs = nN * b
     unsigned spmv_grid = 1, upd_grid = 1, vec_grid = 1, upd2_grid = 1;
@@ -803,7 +811,7 @@ int Solver::solve_b(double *x64) {
         SFEM_TRY(alloc(&v.p, nd, "p"));
         SFEM_TRY(alloc(&v.q, nd, "q"));
         v.minv = minv64;
-        SFEM_CUDA(ctx, cudaMemcpyAsync(v.r, bvec, sizeof(double) * nd, cudaMemcpyDeviceToDevice, ctx->stream));
+        SFEM_CUDA(ctx, cudaMemcpyAsync(v.r, r0vec, sizeof(double) * nd, cudaMemcpyDeviceToDevice, ctx->stream));
         if (block)
             k_init<double, B, 1><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
         else
@@ -832,7 +840,7 @@ int Solver::solve_b(double *x64) {
         SFEM_CUDA(ctx, cudaMemsetAsync(v.x, 0, sizeof(float) * nd, ctx->stream));
         k_cast<float><<<(unsigned)sfem_cdiv(m->nN * mwidth, 256), 256, 0, ctx->stream>>>(m->nN * mwidth, minv64,
                                                                                            v.minv);
-        k_cast<float><<<vec_grid, 256, 0, ctx->stream>>>(nd, bvec, v.r);
+        k_cast<float><<<vec_grid, 256, 0, ctx->stream>>>(nd, r0vec, v.r);
         SFEM_LAUNCHED(ctx);
         SFEM_LAUNCHED(ctx);
         if (block)
@@ -846,7 +854,7 @@ int Solver::solve_b(double *x64) {
 }
 
 int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_vals, const double *f, double *u_out,
-                int mem_space, sfem_solve_stats *stats) {
+                int mem_space, sfem_solve_stats *stats, const double *u0) {
     auto t0 = std::chrono::steady_clock::now();
     const int b = m->b;
     const int64_t n = K->n;
@@ -929,6 +937,27 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
         SFEM_TRY(read_scalars(&hs));
     }
     const double bb = hs.rr;
+    // warm start: x = x0 on the free DOFs, r0 = b - K x0
+    r0vec = bvec;
+    double rr0 = bb;
+    if (u0) {
+        double *ug0 = nullptr, *kx = nullptr;
+        SFEM_TRY(alloc(&ug0, n, "initial guess"));
+        SFEM_TRY(alloc(&kx, nd, "K x0"));
+        SFEM_TRY(alloc(&r0vec, nd, "initial residual"));
+        SFEM_TRY(sfem_copy_in(ctx, ug0, u0, sizeof(double) * n, mem_space));
+        k_gather_global<<<(unsigned)sfem_cdiv(n > 0 ? n : 1, 256), 256, 0, ctx->stream>>>(ug0, n, m->g2i, x64);
+        k_zero_fixed<<<vec_grid, 256, 0, ctx->stream>>>(nd, fixed, x64);
+        ctx->launches += 2;
+        if (b == 1) launch_spmv<double, 1>(K->val, x64, kx, false);
+        else if (b == 2) launch_spmv<double, 2>(K->val, x64, kx, false);
+        else launch_spmv<double, 3>(K->val, x64, kx, false);
+        k_rhs<<<vec_grid, 256, 0, ctx->stream>>>(nd, bvec, kx, fixed, r0vec);
+        k_true_residual<<<vec_grid, UPD_T, 0, ctx->stream>>>(nd, bvec, kx, fixed, S, partial);
+        ctx->launches += 2;
+        SFEM_TRY(read_scalars(&hs));
+        rr0 = hs.rr;
+    }
     int64_t n_free = 0;
     {
         std::vector<unsigned char> hf(nd);
@@ -939,10 +968,11 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
     hs.bb = bb;
     hs.tol2 = opts.rtol * opts.rtol * bb;
     hs.delta2 = opts.reliable_delta * opts.reliable_delta;
-    hs.rr = bb;
-    hs.rr_ref = bb;
+    hs.rr = rr0;
+    hs.rr_ref = rr0;
     hs.it = 0;
-    hs.done = bb > 0.0 && n_free > 0 ? 0 : 1;
+    hs.done = bb > 0.0 && n_free > 0 && rr0 > hs.tol2 ? 0 : 1;
+    if (hs.done) relres = bb > 0.0 ? sqrt(rr0 / bb) : 0.0;
     hs.status = SFEM_OK;
     SFEM_CUDA(ctx, cudaMemcpyAsync(S, &hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
     if (!hs.done) {
@@ -1009,4 +1039,132 @@ extern "C" int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t
     if (stats) memset(stats, 0, sizeof(*stats));
     Solver s(ctx, K, o);
     return s.run(fixed_dofs, nfix, fixed_vals, f, u_out, mem_space, stats);
+}
+
+namespace {
+
+// x0 = sum_j c[j] * u_j over up to three earlier solutions
+__global__ void k_combine3(int64_t n, const double *__restrict__ u0, const double *__restrict__ u1,
+                           const double *__restrict__ u2, double c0, double c1, double c2, double *__restrict__ x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = c0 * u0[i];
+    if (u1) v += c1 * u1[i];
+    if (u2) v += c2 * u2[i];
+    x[i] = v;
+}
+
+// Affine weights (sum 1) of the k earlier prescribed-value vectors G[0..k)
+// that best reproduce g in the least-squares sense; the displacement is an
+// affine function of the prescribed values, so the same weights applied to
+// the earlier solutions give the new one exactly when g lies in their span.
+int affine_weights(const std::vector<const double *> &G, const double *g, int64_t nfix, double *c) {
+    const int k = (int)G.size();
+    if (k == 1) {
+        c[0] = 1.0;
+        return 1;
+    }
+    // unknowns c_1..c_{k-1}, c_0 = 1 - sum; minimise |sum_j c_j (G_j - G_0) - (g - G_0)|
+    double A[2][2] = {{0, 0}, {0, 0}}, r[2] = {0, 0};
+    for (int64_t t = 0; t < nfix; ++t) {
+        double d[2];
+        for (int j = 1; j < k; ++j) d[j - 1] = G[j][t] - G[0][t];
+        const double tt = g[t] - G[0][t];
+        for (int a = 0; a < k - 1; ++a) {
+            r[a] += d[a] * tt;
+            for (int b = 0; b < k - 1; ++b) A[a][b] += d[a] * d[b];
+        }
+    }
+    double x[2] = {0, 0};
+    if (k == 2) {
+        if (!(A[0][0] > 0.0)) return affine_weights({G[0]}, g, nfix, c);
+        x[0] = r[0] / A[0][0];
+    } else {
+        const double det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+        const double scale = A[0][0] * A[1][1];
+        if (!(scale > 0.0) || !(fabs(det) > 1e-12 * scale)) return affine_weights({G[0], G[1]}, g, nfix, c);
+        x[0] = (r[0] * A[1][1] - r[1] * A[0][1]) / det;
+        x[1] = (A[0][0] * r[1] - A[1][0] * r[0]) / det;
+    }
+    c[0] = 1.0;
+    for (int j = 1; j < k; ++j) {
+        c[j] = x[j - 1];
+        c[0] -= x[j - 1];
+    }
+    return k;
+}
+
+}  // namespace
+
+extern "C" int sfem_solve_increments(sfem_ctx *ctx, sfem_matrix *K, const int64_t *fixed_dofs, int64_t nfix,
+                                     const double *fixed_vals, int64_t nsteps, const double *f, double *u_out,
+                                     int mem_space, const sfem_solve_opts *opts, int warm_start,
+                                     sfem_solve_stats *stats) {
+    if (!ctx || !K || !u_out || nsteps < 0) return SFEM_BAD_ARG;
+    if (nfix < 0 || (nfix > 0 && (!fixed_dofs || !fixed_vals)))
+        return sfem_set_error(ctx, SFEM_BAD_ARG, "bad fixed DOF list");
+    if (nsteps == 0) return SFEM_OK;
+    cudaSetDevice(ctx->device);
+    sfem_solve_opts o;
+    sfem_solve_opts_default(&o);
+    if (opts) o = *opts;
+    SFEM_TRY(sfem_check_ptr(ctx, fixed_dofs, mem_space));
+    SFEM_TRY(sfem_check_ptr(ctx, fixed_vals, mem_space));
+    SFEM_TRY(sfem_check_ptr(ctx, f, mem_space));
+    SFEM_TRY(sfem_check_ptr(ctx, u_out, mem_space));
+    const int64_t n = K->n;
+    // the prescribed values of every step: on the host for the warm-start
+    // weights, on the device for the solves
+    std::vector<double> hvals((size_t)(nfix * nsteps));
+    if (nfix > 0)
+        SFEM_CUDA(ctx, cudaMemcpy(hvals.data(), fixed_vals, sizeof(double) * nfix * nsteps, cudaMemcpyDefault));
+    int64_t *dfix = nullptr;
+    double *dvals = nullptr, *df = nullptr, *ring = nullptr, *x0 = nullptr;
+    int st = SFEM_OK;
+    do {
+        if ((st = sfem_dalloc(ctx, (void **)&dfix, sizeof(int64_t) * (nfix ? nfix : 1), "fixed dofs"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&dvals, sizeof(double) * (nfix * nsteps ? nfix * nsteps : 1),
+                              "fixed values")))
+            break;
+        if ((st = sfem_dalloc(ctx, (void **)&ring, sizeof(double) * 3 * (n ? n : 1), "earlier solutions"))) break;
+        if ((st = sfem_dalloc(ctx, (void **)&x0, sizeof(double) * (n ? n : 1), "initial guess"))) break;
+        if ((st = sfem_copy_in(ctx, dfix, fixed_dofs, sizeof(int64_t) * nfix, mem_space))) break;
+        if ((st = sfem_copy_in(ctx, dvals, hvals.data(), sizeof(double) * nfix * nsteps, SFEM_MEM_HOST))) break;
+        if (f) {
+            if ((st = sfem_dalloc(ctx, (void **)&df, sizeof(double) * (n ? n : 1), "f"))) break;
+            if ((st = sfem_copy_in(ctx, df, f, sizeof(double) * n, mem_space))) break;
+        }
+        for (int64_t s = 0; s < nsteps && st == SFEM_OK; ++s) {
+            const double *guess = nullptr;
+            const int64_t kprev = std::min<int64_t>(s, 3);
+            if (warm_start && kprev > 0) {
+                std::vector<const double *> G;
+                const double *U[3] = {nullptr, nullptr, nullptr};
+                for (int64_t j = 0; j < kprev; ++j) {  // most recent first
+                    G.push_back(hvals.data() + (s - 1 - j) * nfix);
+                    U[j] = ring + ((s - 1 - j) % 3) * n;
+                }
+                double c[3] = {0, 0, 0};
+                const int used = affine_weights(G, hvals.data() + s * nfix, nfix, c);
+                k_combine3<<<(unsigned)sfem_cdiv(n > 0 ? n : 1, 256), 256, 0, ctx->stream>>>(
+                    n, U[0], used > 1 ? U[1] : nullptr, used > 2 ? U[2] : nullptr, c[0], c[1], c[2], x0);
+                SFEM_LAUNCHED(ctx);
+                guess = x0;
+            }
+            double *us = ring + (s % 3) * n;
+            sfem_solve_stats one;
+            memset(&one, 0, sizeof(one));
+            {
+                Solver solver(ctx, K, o);
+                st = solver.run(dfix, nfix, dvals + s * nfix, df, us, SFEM_MEM_DEVICE, &one, guess);
+            }
+            if (stats) stats[s] = one;
+            if (st != SFEM_OK) break;
+            st = sfem_copy_out(ctx, u_out + s * n, us, sizeof(double) * n, mem_space);
+        }
+        if (st == SFEM_OK) st = sfem_check_device(ctx, "load increments");
+    } while (0);
+    void *bufs[] = {dfix, dvals, df, ring, x0};
+    for (void *p : bufs) sfem_dfree(ctx, p);
+    return st;
 }

@@ -302,6 +302,41 @@ class Matrix:
         check(code, self.ctx.h)
         return out, stats.as_dict()
 
+    def solve_increments(self, fixed_dofs, fixed_vals, f=None, warm_start=True, **kw):
+        """The driver's load-increment loop (examples/vector3D.jl:310-338) on
+        this K: ``fixed_vals`` is (nsteps, nfix), one row of prescribed
+        values per step, for the same ``fixed_dofs``.  Returns ``(U, stats)``
+        with ``U`` of shape (nsteps, n).  ``warm_start`` starts each step from
+        the best affine combination of earlier solutions."""
+        fd = np.ascontiguousarray(np.asarray(fixed_dofs, dtype=np.int64).ravel())
+        fv = np.ascontiguousarray(np.atleast_2d(np.asarray(fixed_vals, dtype=np.float64)))
+        nsteps = fv.shape[0]
+        if fv.shape[1] != fd.size:
+            raise SfemError(L.SFEM_BAD_ARG, "fixed_vals must be (nsteps, len(fixed_dofs))")
+        F = _Buf(f, np.float64)
+        U = np.empty((nsteps, self.n))
+        stats = (L.SolveStats * max(nsteps, 1))()
+        opts = _solve_opts(**kw)
+        check(lib().sfem_solve_increments(self.ctx.h, self.h, fd.ctypes.data if fd.size else None, fd.size,
+                                          fv.ctypes.data if fv.size else None, nsteps, F.ptr, U.ctypes.data,
+                                          L.MEM_HOST, C.byref(opts), 1 if warm_start else 0, stats),
+              self.ctx.h)
+        return U, [stats[i].as_dict() for i in range(nsteps)]
+
+    def add_penalty(self, NodeList, IEN_faces, beta):
+        """``K <- K + beta * b`` in place on the GPU, b the surface penalty of
+        ``apply_boundary_conditions`` (examples/vector3D.jl:175-264,306-308).
+
+        ``NodeList`` (3, nNodes): the coordinates the faces are integrated
+        on; ``IEN_faces`` (nFaces, 4), 1-based, in the reference's order
+        ``[IEN_btm; IEN_top]``.
+        """
+        X = _Buf(NodeList, np.float64)
+        F = _Buf(IEN_faces, np.int64)
+        check(lib().sfem_penalty_add(self.ctx.h, self.h, X.ptr, F.ptr, int(np.shape(IEN_faces)[0]),
+                                     int(np.shape(IEN_faces)[1]), float(beta), _space(X, F)), self.ctx.h)
+        return self
+
     def close(self):
         if getattr(self, "h", None):
             lib().sfem_matrix_destroy(self.h)
@@ -566,6 +601,48 @@ def assemble_system(ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1, ID=None
         return K.to_scipy()
     finally:
         K.close()
+
+
+def apply_boundary_conditions(ne, NodeList, IEN, IEN_top, IEN_btm, ndim, FunctionClass="Q1", ID=None,
+                              nDof=3, ctx=None):
+    """``apply_boundary_conditions`` of examples/vector3D.jl:175-264 on the GPU.
+
+    Returns the surface penalty matrix ``b`` as ``scipy.sparse.csc_matrix``
+    with the reference's pattern: every DOF pair of every top/bottom face
+    node pair, the off-diagonal DOF pairs as explicit zeros.  It is computed
+    by adding the penalty (beta = 1) to an all-zero matrix with K's pattern;
+    for the driver's ``K_bar = K + beta*b`` keep K on the GPU and call
+    :meth:`Matrix.add_penalty` instead.  3D Q1 only, as the reference.
+    """
+    if ndim != 3 or FunctionClass != "Q1" or nDof != 3:
+        raise SfemError(L.SFEM_UNSUPPORTED, "the reference's surface penalty exists for 3D Q1 "
+                                            "elasticity only")
+    ctx = ctx or get_context()
+    nface = int(ne) ** (ndim - 1)
+    faces = np.concatenate([np.asarray(IEN_btm, np.int64)[:nface], np.asarray(IEN_top, np.int64)[:nface]])
+    Z = assemble_system(ne, NodeList, IEN, ndim, FunctionClass, nDof, ID, 0.0, 0.3, ctx=ctx, as_handle=True)
+    try:
+        Z.add_penalty(NodeList, faces, 1.0)
+        b = Z.to_scipy()
+    finally:
+        Z.close()
+    # keep the entries of node pairs that share a face (the reference's COO triplets)
+    ID = np.asarray(ID, np.int64)
+    dof_node = np.empty(ID.size, np.int64)
+    dof_node[ID.ravel(order="C") - 1] = np.repeat(np.arange(ID.shape[0]), ID.shape[1])
+    pairs = set()
+    for f in faces - 1:
+        for a in f:
+            for c in f:
+                pairs.add((int(a), int(c)))
+    coo = b.tocoo()
+    keep = np.array([(int(dof_node[r]), int(dof_node[c])) in pairs for r, c in zip(coo.row, coo.col)],
+                    dtype=bool)
+    import scipy.sparse as sp
+    n = int(max(ID[faces - 1].max(), 1))
+    out = sp.csc_matrix((coo.data[keep], (coo.row[keep], coo.col[keep])), shape=(n, n))
+    out.sort_indices()
+    return out
 
 
 def solve_dirichlet(K, fixed_dofs, fixed_vals, f=None, **opts):

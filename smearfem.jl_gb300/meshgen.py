@@ -173,6 +173,42 @@ def quad_problem(ne, seed, jitter=0.15, nu=None, nu_range=(0.2, 0.45), e_sigma=N
                    fixed[order], vals[order], plane, rtol, seed)
 
 
+def inflate_sphere(NodeList, x0, x1, y0, y1):
+    """Map every node's (x, y) radially so the square cross-section becomes a
+    disc of the same half-width (src/PostProcess.jl:30-44); returns a new
+    array (the reference mutates its argument)."""
+    out = np.array(NodeList, dtype=np.float64, copy=True)
+    d = out[:2] - np.array([[0.5 * (x0 + x1)], [0.5 * (y0 + y1)]])
+    scale = np.abs(d).max(axis=0)
+    r = np.sqrt(d[0] ** 2 + d[1] ** 2)
+    nz = scale != 0.0                      # Julia's `scale ≈ 0.` holds only for exact 0
+    out[:2, ~nz] = 0.0
+    out[:2, nz] = scale[nz] * d[:, nz] / r[nz]
+    return out
+
+
+def squeeze_increments(NodeList, deltas):
+    """Prescribed z-displacements of the squeeze-flow driver
+    (examples/vector3D.jl:133-173, :312-313): z-DOF 0 on nodes with z == 0
+    and -d on nodes with z == 1 (exact compares), for every d in ``deltas``.
+    Returns ``(fixed_dofs, fixed_vals)`` with ``fixed_vals`` (len(deltas), nfix)."""
+    z = np.asarray(NodeList)[2]
+    nodes = np.flatnonzero((z == 0.0) | (z == 1.0))
+    fixed = 3 * nodes + 3
+    top = z[nodes] == 1.0
+    vals = np.where(top[None, :], -np.asarray(deltas, dtype=np.float64)[:, None], 0.0)
+    return fixed.astype(np.int64), vals
+
+
+def squeeze_problem(ne=8, Young=40.0, nu=0.4):
+    """The reference driver's case (examples/vector3D.jl:266-308): unit cube,
+    ne^3 hexes, E = 40, nu = 0.4; the penalty faces on the inflated cylinder."""
+    NodeList, IEN, ID, IEN_top, IEN_btm = meshgrid(0, 1, 0, 1, 0, 1, ne, 3)
+    cyl = inflate_sphere(NodeList, 0, 1, 0, 1)
+    faces = np.concatenate([IEN_btm, IEN_top])
+    return NodeList, IEN, ID, IEN_top, IEN_btm, cyl, faces
+
+
 # ---- the five benchmark workloads ------------------------------------------
 
 def config1():
