@@ -294,6 +294,43 @@ SFEM_API int sfem_batch_get_launch(const sfem_batch *batch, int *threads, int *c
                                    int *cluster, int64_t *cluster_min_nodes, int *last_grid);
 SFEM_API int sfem_batch_destroy(sfem_batch *batch);
 
+/* ---- on-device mesh generation --------------------------------------------- */
+
+/* The reference's structured grid generator (examples/vector3D.jl:10-130) on
+ * the GPU.  Outputs in the reference's Julia layouts, 1-based, column-major,
+ * any may be NULL: NodeList ndim x (ne+1)^ndim; IEN ne^ndim x 2^ndim; ID
+ * (ne+1)^ndim x ndim with ID[m,l] = ndim(m-1)+l; IEN_top / IEN_btm
+ * ne^(ndim-1) x 2^(ndim-1) (left zero where the reference leaves them:
+ * IEN_top when ne = 1).  Coordinates are linspace-rounded, boundary planes
+ * exact.  z0/z1 are ignored in 2D. */
+SFEM_API int sfem_meshgrid(sfem_ctx *ctx, double x0, double x1, double y0, double y1, double z0, double z1,
+                           int64_t ne, int ndim, double *NodeList, int64_t *IEN, int64_t *ID, int64_t *IEN_top,
+                           int64_t *IEN_btm, int mem_space);
+/* inflate_sphere (src/PostProcess.jl:30-44), in place like the reference:
+ * each node's (x, y) moves radially about the centre of [x0,x1]x[y0,y1] so
+ * that a square ring of half-width s lands on the circle of radius s. */
+SFEM_API int sfem_inflate_sphere(sfem_ctx *ctx, double *NodeList, int ndim, int64_t nNodes, double x0, double x1,
+                                 double y0, double y1, int mem_space);
+
+/* ---- VTK output ------------------------------------------------------------ */
+
+/* write_vtk (src/PostProcess.jl:258-279): one VTK XML UnstructuredGrid file
+ * (.vtu, appended raw data) with the mesh and one point field of ncomp
+ * components (field: ncomp x nNodes column-major, NULL for none).  Cells by
+ * nen: 8 hexahedron, 4 quad, 2 line; 2D points get z = 0.  With host arrays
+ * (SFEM_MEM_HOST) no GPU is needed and ctx may be NULL. */
+SFEM_API int sfem_vtk_write(sfem_ctx *ctx, const char *path, const double *NodeList, int ndim, int64_t nNodes,
+                            const int64_t *IEN, int64_t nEl, int nen, const char *field_name, const double *field,
+                            int ncomp, int mem_space);
+/* write_scene (src/PostProcess.jl:281-304): step i (1-based) of fields
+ * (nsteps blocks of ncomp x nNodes) to <basename>timestep_<i>.vtu as point
+ * field "u", and <basename>displacement.pvd listing them at times 0, 1, ...
+ * Device fields are copied through two pinned buffers, each step's copy
+ * overlapping the previous step's write. */
+SFEM_API int sfem_vtk_write_scene(sfem_ctx *ctx, const char *basename, const double *NodeList, int ndim,
+                                  int64_t nNodes, const int64_t *IEN, int64_t nEl, int nen, const double *fields,
+                                  int ncomp, int64_t nsteps, int mem_space);
+
 /* ---- load increments ------------------------------------------------------ */
 
 /* The driver's load-increment loop (examples/vector3D.jl:310-338): one K,

@@ -118,6 +118,14 @@ SIGNATURES = {
     "sfem_solve_dirichlet": (C.c_int, [P, P, P, I64, P, P, P, C.c_int, C.POINTER(SolveOpts),
                                        C.POINTER(SolveStats)]),
     "sfem_penalty_add": (C.c_int, [P, P, P, P, I64, C.c_int, C.c_double, C.c_int]),
+    "sfem_vtk_write": (C.c_int, [P, C.c_char_p, P, C.c_int, I64, P, I64, C.c_int, C.c_char_p, P, C.c_int,
+                                 C.c_int]),
+    "sfem_vtk_write_scene": (C.c_int, [P, C.c_char_p, P, C.c_int, I64, P, I64, C.c_int, P, C.c_int, I64,
+                                       C.c_int]),
+    "sfem_meshgrid": (C.c_int, [P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                I64, C.c_int, P, P, P, P, P, C.c_int]),
+    "sfem_inflate_sphere": (C.c_int, [P, P, C.c_int, I64, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_int]),
     "sfem_solve_increments": (C.c_int, [P, P, P, I64, P, I64, P, P, C.c_int, C.POINTER(SolveOpts), C.c_int,
                                         P]),
     "sfem_server_config_default": (None, [C.POINTER(ServerConfig)]),

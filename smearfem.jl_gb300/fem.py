@@ -66,6 +66,13 @@ class _Buf:
         self.ptr = C.c_void_p(a.ctypes.data) if a.size else None
 
 
+def _to_dev(v, like):
+    """A scalar or host array as a float64 CUDA tensor on ``like``'s device."""
+    if _is_dev(v):
+        return v
+    return _torch.as_tensor(np.atleast_1d(np.asarray(v, dtype=np.float64)), device=like.device)
+
+
 def _space(*bufs):
     spaces = {b.space for b in bufs if b.ptr is not None}
     if len(spaces) > 1:
@@ -583,6 +590,10 @@ def assemble_system(ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1, ID=None
     X = _Buf(NodeList, np.float64)
     E = _Buf(IEN, np.int64)
     I = _Buf(ID, np.int64) if int(nDof) > 1 else _Buf(None, np.int64)
+    # material values follow the mesh into device memory when the mesh lives there
+    on_dev = X.space == L.MEM_DEVICE
+    Young = _to_dev(Young, NodeList) if on_dev else Young
+    nu = _to_dev(nu, NodeList) if on_dev else nu
     Y = _Buf(np.atleast_1d(Young) if not _is_dev(Young) else Young, np.float64)
     V = _Buf(np.atleast_1d(nu) if not _is_dev(nu) else nu, np.float64)
     space = _space(X, E, I, Y, V)
@@ -601,6 +612,110 @@ def assemble_system(ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1, ID=None
         return K.to_scipy()
     finally:
         K.close()
+
+
+def meshgrid(x0, x1, y0, y1, z0, z1, ne, ndim, device=False, ctx=None):
+    """The reference's ``meshgrid`` (examples/vector3D.jl:10-130) generated on
+    the GPU.  Returns ``(NodeList, IEN, ID, IEN_top, IEN_btm)`` in the
+    reference's shapes, 1-based: numpy arrays, or with ``device=True`` CUDA
+    tensors that stay on the GPU (the other entry points take them as they
+    are, so no host copy of the mesh is made)."""
+    ctx = ctx or get_context()
+    ne, ndim = int(ne), int(ndim)
+    n1 = ne + 1
+    nN, nEl, nF, nenF = n1 ** ndim, ne ** ndim, ne ** (ndim - 1), 2 ** (ndim - 1)
+    # (rows, cols) of each output in the reference's Julia shapes; stored column-major
+    shapes = [(ndim, nN, np.float64), (nEl, 2 ** ndim, np.int64), (nN, ndim, np.int64), (nF, nenF, np.int64),
+              (nF, nenF, np.int64)]
+    tdt = {np.float64: _torch.float64, np.int64: _torch.int64}
+    if device:
+        dev = _torch.device("cuda", ctx.device)
+        bufs = [_torch.empty(r * c, dtype=tdt[t], device=dev) for r, c, t in shapes]
+        ptrs = [C.c_void_p(b.data_ptr()) for b in bufs]
+        space = L.MEM_DEVICE
+    else:
+        bufs = [np.empty(r * c, dtype=t) for r, c, t in shapes]
+        ptrs = [C.c_void_p(b.ctypes.data) for b in bufs]
+        space = L.MEM_HOST
+    check(lib().sfem_meshgrid(ctx.h, float(x0), float(x1), float(y0), float(y1), float(z0), float(z1), ne,
+                              ndim, *ptrs, space), ctx.h)
+    return tuple(b.view(c, r).t() if device else b.reshape(c, r).T for b, (r, c, _t) in zip(bufs, shapes))
+
+
+def inflate_sphere(NodeList, x0, x1, y0, y1, ctx=None):
+    """``inflate_sphere`` (src/PostProcess.jl:30-44) on the GPU.  A CUDA
+    tensor is changed in place (as the reference changes its argument);
+    a numpy array is returned as a new array."""
+    ctx = ctx or get_context()
+    if _is_dev(NodeList):
+        X = NodeList
+        flat = X.t().contiguous() if not X.t().is_contiguous() else X.t()
+        check(lib().sfem_inflate_sphere(ctx.h, C.c_void_p(flat.data_ptr()), int(X.shape[0]), int(X.shape[1]),
+                                        float(x0), float(x1), float(y0), float(y1), L.MEM_DEVICE), ctx.h)
+        if flat.data_ptr() != X.t().data_ptr():
+            X.copy_(flat.t())
+        return X
+    out = np.array(NodeList, dtype=np.float64, order="F", copy=True)
+    check(lib().sfem_inflate_sphere(ctx.h, C.c_void_p(out.ctypes.data), int(out.shape[0]), int(out.shape[1]),
+                                    float(x0), float(x1), float(y0), float(y1), L.MEM_HOST), ctx.h)
+    return out
+
+
+def _field_ncomp(q, nN):
+    shape = tuple(q.shape)
+    if len(shape) == 1:
+        if shape[0] != nN:
+            raise SfemError(L.SFEM_BAD_ARG, "a vector field has one value per node")
+        return 1
+    if shape[1] != nN:
+        raise SfemError(L.SFEM_BAD_ARG, "a matrix field is (components, nNodes)")
+    return shape[0]
+
+
+def write_vtk(fileName, fieldName, NodeList, IEN, ne, ndim, q, ctx=None):
+    """``write_vtk`` of src/PostProcess.jl:258-279: ``fileName`` + ".vtu" with
+    cells ``IEN[1:ne^ndim, :]`` and the point field ``q`` (nNodes values, or
+    a (components, nNodes) matrix like the driver's ``motion``).  Host
+    arrays are written without a GPU; CUDA tensors are copied from it."""
+    nEl = int(ne) ** int(ndim)
+    X, E, Q = _Buf(NodeList, np.float64), _Buf(np.asarray(IEN)[:nEl] if not _is_dev(IEN) else IEN[:nEl],
+                                               np.int64), _Buf(q, np.float64)
+    space = _space(X, E, Q)
+    nN = int(np.shape(NodeList)[1])
+    ncomp = _field_ncomp(q, nN)
+    h = get_context().h if space == L.MEM_DEVICE else (ctx.h if ctx else None)
+    check(lib().sfem_vtk_write(h, (str(fileName) + ".vtu").encode(), X.ptr, int(np.shape(NodeList)[0]), nN, E.ptr,
+                               nEl, int(np.shape(IEN)[1]), str(fieldName).encode(), Q.ptr, ncomp, space), h)
+
+
+def write_scene(fileName, NodeList, IEN, ne, ndim, fields, ctx=None):
+    """``write_scene`` of src/PostProcess.jl:281-304: one ``<fileName>timestep_i.vtu``
+    per field (point data "u") and ``<fileName>displacement.pvd`` with the
+    steps at times 0, 1, ...  ``fields``: a list of equally shaped arrays, or
+    one (nsteps, components, nNodes) array or CUDA tensor."""
+    nEl = int(ne) ** int(ndim)
+    nN = int(np.shape(NodeList)[1])
+    if _is_dev(fields):
+        F = fields.contiguous()
+        nsteps = int(F.shape[0])
+        ncomp = _field_ncomp(F[0], nN) if nsteps else 1
+        # each step (components, nNodes) must be column-major: (nNodes, components) rows
+        F = F.transpose(1, 2).contiguous() if F.dim() == 3 else F
+        Fp, space = C.c_void_p(F.data_ptr()), L.MEM_DEVICE
+        keep = F
+    else:
+        arr = [np.asarray(f, dtype=np.float64) for f in fields]
+        nsteps = len(arr)
+        ncomp = _field_ncomp(arr[0], nN) if nsteps else 1
+        keep = np.concatenate([f.ravel(order="F") for f in arr]) if nsteps else np.zeros(1)
+        Fp, space = C.c_void_p(keep.ctypes.data), L.MEM_HOST
+    X, E = _Buf(NodeList, np.float64), _Buf(np.asarray(IEN)[:nEl] if not _is_dev(IEN) else IEN[:nEl], np.int64)
+    if _space(X, E) != space:
+        raise SfemError(L.SFEM_BAD_ARG, "mesh and fields must be in the same memory space")
+    h = get_context().h if space == L.MEM_DEVICE else (ctx.h if ctx else None)
+    check(lib().sfem_vtk_write_scene(h, str(fileName).encode(), X.ptr, int(np.shape(NodeList)[0]), nN, E.ptr, nEl,
+                                     int(np.shape(IEN)[1]), Fp, ncomp, nsteps, space), h)
+    del keep
 
 
 def apply_boundary_conditions(ne, NodeList, IEN, IEN_top, IEN_btm, ndim, FunctionClass="Q1", ID=None,
