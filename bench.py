@@ -55,8 +55,9 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ne", type=int, default=128)
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--legs", default="value,mixed,e2e,cpu,batch,serve",
-                    help="comma list of value,mixed,e2e,cpu,batch,serve (profiling runs pick one)")
+    ap.add_argument("--legs", default="value,mixed,e2e,cpu,precision,batch,serve",
+                    help="comma list of value,mixed,e2e,cpu,precision,batch,serve (profiling runs pick one)")
+    ap.add_argument("--precision-ne", type=int, default=96, help="mesh size of the precision leg")
     ap.add_argument("--batch-count", type=int, default=1024, help="meshes in the batch leg")
     ap.add_argument("--batch-rtol", type=float, default=1e-12,
                     help="batch-leg relative residual (1e-12 keeps the error in u under 1e-8)")
@@ -422,6 +423,8 @@ def our_arm(args, dist):
         line["e2e"] = {"value": ve2e, "unit": UNIT, "ms_per_step": mse,
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hU.nbytes),
                        "rel_err": float(np.linalg.norm(hU - uref_h) / np.linalg.norm(uref_h))}
+    if "precision" in args.legs:
+        line["precision"] = precision_leg(args, pkg, ctx, stream, dist)
     if "batch" in args.legs:
         line["batch"] = batch_leg(args, pkg, ctx, stream, dist)
     if "serve" in args.legs:
@@ -434,6 +437,64 @@ def our_arm(args, dist):
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def precision_leg(args, pkg, ctx, stream, dist):
+    """Precision workload: 96^3 jittered hex mesh, per-element E ~ lognormal(0, 1)
+    (stiffness contrast ~1e3), nu ~ U(0.25, 0.45) per element, 4-mode top
+    displacement.  Plain FP64 Jacobi-PCG against FP32-inner block-Jacobi PCG
+    with FP64 residual refreshes, both to 1e-10 relative residual; the mixed
+    result's error is measured against a tight FP64 solve (1e-13)."""
+    import torch
+    p = pkg.meshgen.config3(ne=args.precision_ne)
+    dev = torch.device("cuda", ctx.device)
+    NLf, IENf, IDf = (np.asfortranarray(a) for a in (p.NodeList, p.IEN, p.ID))
+    dX = torch.from_numpy(NLf.ravel(order="F")).to(dev)
+    dIEN = torch.from_numpy(IENf.ravel(order="F")).to(dev)
+    dID = torch.from_numpy(IDf.ravel(order="F")).to(dev)
+    dY = torch.from_numpy(p.Young).to(dev)
+    dNU = torch.from_numpy(np.ascontiguousarray(p.nu)).to(dev)
+    dFD = torch.from_numpy(p.fixed_dofs).to(dev)
+    dFV = torch.from_numpy(p.fixed_vals).to(dev)
+    nN, nEl = p.n_nodes, p.n_elem
+    dU = torch.empty(p.n_dof, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+
+    def step(precision, precond, rtol, out=dU):
+        m = pkg.Mesh(p.ne, dX, dIEN, 3, "Q1", 3, dID, ctx=ctx, nNodes=nN, nen=8, ldIEN=nEl)
+        K = m.assemble(dY, dNU)
+        _, st = K.solve(dFD, dFV, precision=precision, precond=precond, rtol=rtol, out=out)
+        K.close()
+        m.close()
+        return st
+
+    uref = torch.empty_like(dU)
+    step("fp64", "jacobi", 1e-13, out=uref)
+    uref_h = uref.cpu().numpy()
+
+    def run(precision, precond):
+        for _ in range(args.warmup):
+            step(precision, precond, 1e-10)
+        dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sts = [step(precision, precond, 1e-10) for _ in range(args.steps)]
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        err = float(np.linalg.norm(dU.cpu().numpy() - uref_h) / np.linalg.norm(uref_h))
+        v, ms = aggregate(dist, p.n_dof, ms)
+        return {"value": v, "unit": UNIT, "ms_per_step": ms, "iterations": sts[-1]["iterations"],
+                "fp64_refreshes": sts[-1]["reliable_updates"], "relres": sts[-1]["relres"], "rel_err": err}
+
+    fp64 = run("fp64", "jacobi")
+    mixed = run("mixed", "block_jacobi")
+    return {"workload": f"{p.ne}^3 Q1 hex elasticity, E ~ lognormal(0, 1), nu ~ U(0.25, 0.45) per element "
+                        "(configs[2]); assemble + Dirichlet + PCG to 1e-10, inputs on the device",
+            "n_dof": p.n_dof, "fp64_jacobi": fp64, "mixed_block_jacobi": mixed,
+            "speedup_mixed_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
+            "rel_err_reference": "FP64 Jacobi-PCG on the GPU to relative residual 1e-13"}
 
 
 def batch_leg(args, pkg, ctx, stream, dist):
