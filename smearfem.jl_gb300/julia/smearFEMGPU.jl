@@ -14,7 +14,8 @@ module smearFEMGPU
 
 using SparseArrays
 
-export assemble_system, gaussian_quadrature, basis_function, solve_dirichlet, GPUMatrix
+export assemble_system, gaussian_quadrature, basis_function, solve_dirichlet, GPUMatrix,
+       apply_boundary_conditions!, solve_increments, meshgrid, inflate_sphere, write_vtk, write_scene
 
 const libsfem = get(ENV, "SMEARFEM_GPU_LIB", joinpath(@__DIR__, "..", "lib", "libsmearfem_gpu.so"))
 
@@ -174,6 +175,126 @@ function solve_dirichlet(K::GPUMatrix, fixed_dofs, fixed_vals, f=nothing; precis
     end
     check(st, ctx)
     return u
+end
+
+"""
+    apply_boundary_conditions!(K::GPUMatrix, NodeList, IEN_top, IEN_btm, β)
+
+`K_bar = K + β*b` in place on the GPU, where `b` is the surface penalty of
+`apply_boundary_conditions` (examples/vector3D.jl:175-264, 306-308) computed on
+the face coordinates `NodeList` (the driver passes the inflated cylinder).
+"""
+function apply_boundary_conditions!(K::GPUMatrix, NodeList, IEN_top, IEN_btm, β)
+    ctx = context()
+    X = convert(Matrix{Float64}, NodeList)
+    F = vcat(convert(Matrix{Int64}, IEN_btm), convert(Matrix{Int64}, IEN_top))   # the reference's COO order
+    GC.@preserve X F begin
+        st = ccall((:sfem_penalty_add, libsfem), Cint,
+                   (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Int64}, Int64, Cint, Cdouble, Cint),
+                   ctx.h, K.h, X, F, size(F, 1), size(F, 2), β, SFEM_MEM_HOST)
+    end
+    check(st, ctx)
+    return K
+end
+
+"""
+    solve_increments(K::GPUMatrix, fixed_dofs, fixed_vals::Matrix; warm_start=true, precision=:fp64,
+                     precond=:jacobi, rtol=1e-10, maxit=100000)
+
+The load-increment loop of examples/vector3D.jl:310-338: column `s` of
+`fixed_vals` (nfix × nsteps) holds step s's prescribed values; returns the
+n × nsteps displacements.  With `warm_start` each step starts from the best
+affine combination of up to three earlier solutions.
+"""
+function solve_increments(K::GPUMatrix, fixed_dofs, fixed_vals::AbstractMatrix; warm_start=true,
+                          precision=:fp64, precond=:jacobi, rtol=1e-10, maxit=100000)
+    ctx = context()
+    fd = Int64.(collect(fixed_dofs)); fv = convert(Matrix{Float64}, fixed_vals)
+    nsteps = size(fv, 2)
+    U = Matrix{Float64}(undef, K.n, nsteps)
+    opts = SolveOpts(precision == :mixed ? 1 : 0, precond == :block_jacobi ? 1 : 0, rtol, maxit, 32, 0.1, 0, 0)
+    GC.@preserve fd fv U begin
+        st = ccall((:sfem_solve_increments, libsfem), Cint,
+                   (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Int64, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Ptr{Cdouble},
+                    Cint, Ref{SolveOpts}, Cint, Ptr{Cvoid}),
+                   ctx.h, K.h, fd, length(fd), fv, nsteps, C_NULL, U, SFEM_MEM_HOST, opts, warm_start ? 1 : 0,
+                   C_NULL)
+    end
+    check(st, ctx)
+    return U
+end
+
+"""
+    meshgrid(x0, x1, y0, y1, z0, z1, ne, ndim)
+
+The driver's mesh generator (examples/vector3D.jl:10-130) run on the GPU:
+`NodeList, IEN, ID, IEN_top, IEN_btm` in the reference's shapes.
+"""
+function meshgrid(x0, x1, y0, y1, z0, z1, ne, ndim)
+    ctx = context()
+    nN = (ne + 1)^ndim; nEl = ne^ndim; nF = ne^(ndim - 1); nenF = 2^(ndim - 1)
+    NodeList = Matrix{Float64}(undef, ndim, nN)
+    IEN = Matrix{Int64}(undef, nEl, 2^ndim); ID = Matrix{Int64}(undef, nN, ndim)
+    IEN_top = Matrix{Int64}(undef, nF, nenF); IEN_btm = Matrix{Int64}(undef, nF, nenF)
+    st = ccall((:sfem_meshgrid, libsfem), Cint,
+               (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble, Cdouble, Cdouble, Cdouble, Int64, Cint,
+                Ptr{Cdouble}, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Cint),
+               ctx.h, x0, x1, y0, y1, z0, z1, ne, ndim, NodeList, IEN, ID, IEN_top, IEN_btm, SFEM_MEM_HOST)
+    check(st, ctx)
+    return NodeList, IEN, ID, IEN_top, IEN_btm
+end
+
+"""
+    inflate_sphere(NodeList, x0, x1, y0, y1)
+
+src/PostProcess.jl:30-44 on the GPU; like the reference it changes `NodeList`
+in place and returns it.
+"""
+function inflate_sphere(NodeList::Matrix{Float64}, x0, x1, y0, y1)
+    ctx = context()
+    st = ccall((:sfem_inflate_sphere, libsfem), Cint,
+               (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Int64, Cdouble, Cdouble, Cdouble, Cdouble, Cint),
+               ctx.h, NodeList, size(NodeList, 1), size(NodeList, 2), x0, x1, y0, y1, SFEM_MEM_HOST)
+    check(st, ctx)
+    return NodeList
+end
+
+"""
+    write_vtk(fileName, fieldName, NodeList, IEN, ne, ndim, q)
+
+src/PostProcess.jl:258-279: `fileName.vtu` with the cells `IEN[1:ne^ndim, :]` and
+the point field `q` (one value per node, or a components × nodes matrix).
+"""
+function write_vtk(fileName, fieldName, NodeList, IEN, ne, ndim, q)
+    X = convert(Matrix{Float64}, NodeList); E = convert(Matrix{Int64}, IEN[1:ne^ndim, :])
+    Q = convert(Array{Float64}, q)
+    ncomp = ndims(Q) == 1 ? 1 : size(Q, 1)
+    st = ccall((:sfem_vtk_write, libsfem), Cint,
+               (Ptr{Cvoid}, Cstring, Ptr{Cdouble}, Cint, Int64, Ptr{Int64}, Int64, Cint, Cstring,
+                Ptr{Cdouble}, Cint, Cint),
+               C_NULL, string(fileName, ".vtu"), X, size(X, 1), size(X, 2), E, size(E, 1), size(E, 2),
+               string(fieldName), Q, ncomp, SFEM_MEM_HOST)
+    st == SFEM_OK || error("smearFEMGPU: writing $fileName.vtu failed (status $st)")
+    return nothing
+end
+
+"""
+    write_scene(fileName, NodeList, IEN, ne, ndim, fields)
+
+src/PostProcess.jl:281-304: `fileName` * "timestep_i.vtu" per field (point data
+"u") and `fileName` * "displacement.pvd" listing them at times 0, 1, ...
+"""
+function write_scene(fileName, NodeList, IEN, ne, ndim, fields)
+    X = convert(Matrix{Float64}, NodeList); E = convert(Matrix{Int64}, IEN[1:ne^ndim, :])
+    F = reduce(vcat, [vec(convert(Array{Float64}, f)) for f in fields])
+    ncomp = ndims(fields[1]) == 1 ? 1 : size(fields[1], 1)
+    st = ccall((:sfem_vtk_write_scene, libsfem), Cint,
+               (Ptr{Cvoid}, Cstring, Ptr{Cdouble}, Cint, Int64, Ptr{Int64}, Int64, Cint, Ptr{Cdouble}, Cint,
+                Int64, Cint),
+               C_NULL, string(fileName), X, size(X, 1), size(X, 2), E, size(E, 1), size(E, 2), F, ncomp,
+               length(fields), SFEM_MEM_HOST)
+    st == SFEM_OK || error("smearFEMGPU: writing the scene $fileName failed (status $st)")
+    return nothing
 end
 
 end # module
