@@ -59,6 +59,8 @@ def parse_args(argv=None):
                     help="comma list of value,mixed,e2e,cpu,precision,batch,serve (profiling runs pick one)")
     ap.add_argument("--precision-ne", type=int, default=96, help="mesh size of the precision leg")
     ap.add_argument("--batch-count", type=int, default=1024, help="meshes in the batch leg")
+    ap.add_argument("--batch-launch", default="",
+                    help="threads,ctas_per_sm,cluster,cluster_min_nodes: fixed batch launch shape (no autotune)")
     ap.add_argument("--batch-rtol", type=float, default=1e-12,
                     help="batch-leg relative residual (1e-12 keeps the error in u under 1e-8)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
@@ -519,8 +521,12 @@ def batch_leg(args, pkg, ctx, stream, dist):
     # tuning trials: full solves of a quarter of the meshes, taken evenly
     # from the size order (capping iterations would hide what clusters buy on
     # the largest meshes)
-    shape, tuned_ms = bt.autotune(1.0, nus, fixed, vals, plane="strain", precision="mixed",
-                                  precond="block_jacobi", rtol=rtol, sample=max(1, len(probs) // 4))
+    if args.batch_launch:
+        bt.set_launch(*[int(x) for x in args.batch_launch.split(",")])
+        shape, tuned_ms = bt.launch(), None
+    else:
+        shape, tuned_ms = bt.autotune(1.0, nus, fixed, vals, plane="strain", precision="mixed",
+                                      precond="block_jacobi", rtol=rtol, sample=max(1, len(probs) // 4))
     t_tune = time.perf_counter() - t0
 
     def run_batch():
