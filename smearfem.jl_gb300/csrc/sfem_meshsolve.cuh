@@ -154,6 +154,87 @@ __device__ __forceinline__ double2 block_sum2(double a, double b, double *sh, in
     return make_double2(x, y);
 }
 
+// FP32 copy of K inside the per-mesh pipeline.  Each lane's block entries of
+// a slab are contiguous -- chunks of four, then the rest -- so a lane reads
+// its block with one (B = 2) or three (B = 3) vector loads while the warp
+// still reads whole contiguous segments: B = 1 one float per lane; B = 2 a
+// float4; B = 3 a float4, a float4 and a float (1152 bytes per slab, no
+// padding).  Fewer load instructions per product: the CG loop of one group
+// is bound by memory latency and load issue, not by bytes.
+template <int B>
+__device__ __forceinline__ int64_t v32_at(int64_t slab, int lane, int e) {
+    if constexpr (B == 1) {
+        return slab * 32 + lane;
+    } else if constexpr (B == 2) {
+        return (slab * 32 + lane) * 4 + e;
+    } else {
+        const int64_t base = slab * 288;
+        return e < 4 ? base + lane * 4 + e : (e < 8 ? base + 128 + lane * 4 + (e - 4) : base + 256 + lane);
+    }
+}
+
+template <int B>
+__device__ __forceinline__ void load_v32(const float *__restrict__ v, int64_t slab, int lane, float *out) {
+    if constexpr (B == 1) {
+        out[0] = __ldcs(v + slab * 32 + lane);
+    } else if constexpr (B == 2) {
+        const float4 t = __ldcs(reinterpret_cast<const float4 *>(v + (slab * 32 + lane) * 4));
+        out[0] = t.x;
+        out[1] = t.y;
+        out[2] = t.z;
+        out[3] = t.w;
+    } else {
+        const float *b = v + slab * 288;
+        const float4 t0 = __ldcs(reinterpret_cast<const float4 *>(b + lane * 4));
+        const float4 t1 = __ldcs(reinterpret_cast<const float4 *>(b + 128 + lane * 4));
+        out[0] = t0.x;
+        out[1] = t0.y;
+        out[2] = t0.z;
+        out[3] = t0.w;
+        out[4] = t1.x;
+        out[5] = t1.y;
+        out[6] = t1.z;
+        out[7] = t1.w;
+        out[8] = __ldcs(b + 256 + lane);
+    }
+}
+
+// Block of K at (slab, lane): FP32 from the per-mesh layout above, FP64 from
+// the sliced-ELL layout (entry-major).
+template <typename T, int B>
+__device__ __forceinline__ void load_block(const T *__restrict__ val, int64_t slab, int lane, T *out) {
+    if constexpr (sizeof(T) == 4) {
+        load_v32<B>(val, slab, lane, out);
+    } else {
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) out[e] = __ldcs(val + (slab * B * B + e) * 32 + lane);
+    }
+}
+
+// The B entries of node c of the multiplied vector (see spmv_operand); 2D
+// FP32 vectors are read as one float2 per array.
+template <bool FUSE_P, typename T, int B>
+__device__ __forceinline__ void gather_node(const T *__restrict__ x, const T *__restrict__ z, T beta, int64_t c,
+                                            T *g) {
+    if constexpr (sizeof(T) == 4 && B == 2) {
+        const float2 xv = *reinterpret_cast<const float2 *>(x + c * 2);
+        if constexpr (FUSE_P) {
+            const float2 zv = *reinterpret_cast<const float2 *>(z + c * 2);
+            g[0] = fmaf(beta, xv.x, zv.x);
+            g[1] = fmaf(beta, xv.y, zv.y);
+        } else {
+            g[0] = xv.x;
+            g[1] = xv.y;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if constexpr (FUSE_P) g[j] = fma(beta, x[c * B + j], z[c * B + j]);
+            else g[j] = x[c * B + j];
+        }
+    }
+}
+
 // Entry idx of the multiplied vector: x itself, or with FUSE_P the CG search
 // direction z + beta * x formed on the fly (x = the previous direction).
 template <bool FUSE_P, typename T>
@@ -226,13 +307,9 @@ __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr,
         if (W > 0 && k1 - k0 == W) {
             T v[WP][B * B], g[WP][B];
 #pragma unroll
-            for (int u = 0; u < WP; ++u)
+            for (int u = 0; u < WP; ++u) load_block<T, B>(val, k0 + u, lane, v[u]);
 #pragma unroll
-                for (int e = 0; e < B * B; ++e) v[u][e] = __ldcs(val + ((k0 + u) * B * B + e) * 32 + lane);
-#pragma unroll
-            for (int u = 0; u < WP; ++u)
-#pragma unroll
-                for (int j = 0; j < B; ++j) g[u][j] = spmv_operand<FUSE_P>(x, z, beta, (int64_t)cn[u] * B + j);
+            for (int u = 0; u < WP; ++u) gather_node<FUSE_P, T, B>(x, z, beta, (int64_t)cn[u], g[u]);
             if (nk1 - nk0 == W) {
 #pragma unroll
                 for (int u = 0; u < WP; ++u) ncn[u] = __ldcs(col + (nk0 + u) * 32 + lane);
@@ -255,13 +332,9 @@ __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr,
 #pragma unroll
                 for (int u = 0; u < U; ++u) c[u] = __ldcs(col + (k + u) * 32 + lane);
 #pragma unroll
-                for (int u = 0; u < U; ++u)
+                for (int u = 0; u < U; ++u) load_block<T, B>(val, k + u, lane, v[u]);
 #pragma unroll
-                    for (int e = 0; e < B * B; ++e) v[u][e] = __ldcs(val + ((k + u) * B * B + e) * 32 + lane);
-#pragma unroll
-                for (int u = 0; u < U; ++u)
-#pragma unroll
-                    for (int j = 0; j < B; ++j) g[u][j] = spmv_operand<FUSE_P>(x, z, beta, (int64_t)c[u] * B + j);
+                for (int u = 0; u < U; ++u) gather_node<FUSE_P, T, B>(x, z, beta, (int64_t)c[u], g[u]);
 #pragma unroll
                 for (int u = 0; u < U; ++u)
 #pragma unroll
@@ -272,10 +345,8 @@ __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr,
             for (; k < k1; ++k) {
                 const int c = __ldcs(col + k * 32 + lane);
                 T v[B * B], g[B];
-#pragma unroll
-                for (int e = 0; e < B * B; ++e) v[e] = __ldcs(val + (k * B * B + e) * 32 + lane);
-#pragma unroll
-                for (int j = 0; j < B; ++j) g[j] = spmv_operand<FUSE_P>(x, z, beta, (int64_t)c * B + j);
+                load_block<T, B>(val, k, lane, v);
+                gather_node<FUSE_P, T, B>(x, z, beta, (int64_t)c, g);
 #pragma unroll
                 for (int i = 0; i < B; ++i)
 #pragma unroll
@@ -563,7 +634,7 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
 #pragma unroll
                 for (int i = 0; i < B * B; ++i) {
                     a.val64[(slab * B * B + i) * 32 + lane] = acc[i];
-                    if (MIXED) a.val32[(slab * B * B + i) * 32 + lane] = (float)acc[i];
+                    if (MIXED) a.val32[v32_at<B>(slab, lane, i)] = (float)acc[i];
                 }
             }
         }
@@ -734,28 +805,38 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                 for (int v = 0; v < NV; ++v) {
                     const int64_t node = nb + v * gstride;
                     if (node < n1) {
+                        if constexpr (sizeof(T) == 4 && B == 2) {  // one vector load per array
+                            const float2 p2 = *reinterpret_cast<const float2 *>(pv + node * 2);
+                            const float2 x2 = *reinterpret_cast<const float2 *>(xv + node * 2);
+                            const float2 q2 = *reinterpret_cast<const float2 *>(qv + node * 2);
+                            const float2 r2 = *reinterpret_cast<const float2 *>(rv + node * 2);
+                            const float4 m4 = *reinterpret_cast<const float4 *>(minv + node * 4);
+                            P[v][0] = p2.x, P[v][1] = p2.y, X[v][0] = x2.x, X[v][1] = x2.y;
+                            Q[v][0] = q2.x, Q[v][1] = q2.y, R[v][0] = r2.x, R[v][1] = r2.y;
+                            Mi[v][0] = m4.x, Mi[v][1] = m4.y, Mi[v][2] = m4.z, Mi[v][3] = m4.w;
+                        } else {
 #pragma unroll
-                        for (int i = 0; i < B; ++i) {
-                            const int64_t d = node * B + i;
-                            P[v][i] = pv[d];
-                            X[v][i] = xv[d];
-                            Q[v][i] = qv[d];
-                            R[v][i] = rv[d];
+                            for (int i = 0; i < B; ++i) {
+                                const int64_t d = node * B + i;
+                                P[v][i] = pv[d];
+                                X[v][i] = xv[d];
+                                Q[v][i] = qv[d];
+                                R[v][i] = rv[d];
+                            }
+#pragma unroll
+                            for (int e = 0; e < B * B; ++e) Mi[v][e] = minv[node * B * B + e];
                         }
-#pragma unroll
-                        for (int e = 0; e < B * B; ++e) Mi[v][e] = minv[node * B * B + e];
                     }
                 }
 #pragma unroll
                 for (int v = 0; v < NV; ++v) {
                     const int64_t node = nb + v * gstride;
                     if (node < n1) {
+                        T Xn[B], Z[B];
 #pragma unroll
                         for (int i = 0; i < B; ++i) {
-                            const int64_t d = node * B + i;
-                            xv[d] = fma(alpha, P[v][i], X[v][i]);
+                            Xn[i] = fma(alpha, P[v][i], X[v][i]);
                             R[v][i] = fma(-alpha, Q[v][i], R[v][i]);
-                            rv[d] = R[v][i];
                             prr += (double)(R[v][i] * R[v][i]);
                         }
 #pragma unroll
@@ -763,8 +844,20 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                             T zi = T(0);
 #pragma unroll
                             for (int j = 0; j < B; ++j) zi = fma(Mi[v][i * B + j], R[v][j], zi);
-                            zv[node * B + i] = zi;
+                            Z[i] = zi;
                             prz += (double)(R[v][i] * zi);
+                        }
+                        if constexpr (sizeof(T) == 4 && B == 2) {
+                            *reinterpret_cast<float2 *>(xv + node * 2) = make_float2(Xn[0], Xn[1]);
+                            *reinterpret_cast<float2 *>(rv + node * 2) = make_float2(R[v][0], R[v][1]);
+                            *reinterpret_cast<float2 *>(zv + node * 2) = make_float2(Z[0], Z[1]);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < B; ++i) {
+                                xv[node * B + i] = Xn[i];
+                                rv[node * B + i] = R[v][i];
+                                zv[node * B + i] = Z[i];
+                            }
                         }
                     }
                 }
