@@ -324,6 +324,81 @@ k_update(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, co
     }
 }
 
+// The same update with one thread per node: a thread loads its node's B
+// entries of x, p, q, r and its nodal inverse block, and keeps them in
+// registers -- no shared-memory staging and no barrier per tile, and B + B*B
+// loads in flight per thread.  A warp's loads still cover contiguous
+// segments (32 consecutive nodes).
+template <typename T, int B, int PC, bool MIXED>
+__global__ void __launch_bounds__(UPD_T)
+k_update_node(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
+              const T *__restrict__ q, const T *__restrict__ minv, CgScalars *S, double *partial) {
+    if (S->done) return;
+    const T alpha = (T)S->alpha;
+    double rz = 0.0, rr = 0.0;
+    for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < nN;
+         node += (int64_t)gridDim.x * blockDim.x) {
+        T xv[B], pv[B], qv[B], rv[B], mv[PC == 0 || B == 1 ? B : B * B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const int64_t d = node * B + i;
+            xv[i] = x[d];
+            pv[i] = p[d];
+            qv[i] = q[d];
+            rv[i] = r[d];
+        }
+        if (PC == 0 || B == 1) {
+#pragma unroll
+            for (int i = 0; i < B; ++i) mv[i] = minv[node * B + i];
+        } else {
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) mv[e] = minv[node * B * B + e];
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const int64_t d = node * B + i;
+            x[d] = fma(alpha, pv[i], xv[i]);
+            rv[i] = fma(-alpha, qv[i], rv[i]);
+            r[d] = rv[i];
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            T zi;
+            if (PC == 0 || B == 1) {
+                zi = mv[i] * rv[i];
+            } else {
+                zi = T(0);
+#pragma unroll
+                for (int j = 0; j < B; ++j) zi = fma(mv[i * B + j], rv[j], zi);
+            }
+            z[node * B + i] = zi;
+            rz += (double)(rv[i] * zi);
+            rr += (double)(rv[i] * rv[i]);
+        }
+    }
+    double trz, trr;
+    if (reduce2_last(rz, rr, partial, &S->ticket[1], &trz, &trr) && threadIdx.x == 0) {
+        S->rr = trr;
+        S->it += 1;
+        S->rz_prev = S->rz;
+        S->rz = trz;
+        S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        if (!(trr == trr)) {
+            S->done = 1;
+            S->status = SFEM_SINGULAR;
+        } else if (MIXED) {
+            if (S->it >= S->maxit) S->maxit_hit = 1;
+            if (trr <= S->tol2 || trr <= S->delta2 * S->rr_ref || S->maxit_hit) S->refresh = 1;
+        } else if (trr <= S->tol2) {
+            S->done = 1;
+            S->status = SFEM_OK;
+        } else if (S->it >= S->maxit) {
+            S->done = 1;
+            S->status = SFEM_NOT_CONVERGED;
+        }
+    }
+}
+
 template <typename T>
 __global__ void k_update_p(int64_t n, T *__restrict__ p, const T *__restrict__ z, const CgScalars *S) {
     if (S->done) return;
@@ -715,8 +790,8 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
         launch_spmv<T, B>(val, v.p, v.q, true);
         if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
         {
-            auto kern = k_update<T, B, PC, MIXED>;
-            kern<<<resident_grid(ctx, kern, UPD_NODES * B, upd2_grid), UPD_NODES * B, 0, ctx->stream>>>(
+            auto kern = k_update_node<T, B, PC, MIXED>;
+            kern<<<resident_grid(ctx, kern, UPD_T, upd_grid), UPD_T, 0, ctx->stream>>>(
                 m->nN, v.x, v.r, v.z, v.p, v.q, v.minv, S, partial);
         }
         SFEM_LAUNCHED(ctx);
