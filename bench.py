@@ -205,7 +205,7 @@ def cpu_sample(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=64, sam
     from oracle import coracle
     coracle.build()
     threads = coracle.max_threads()
-    q = pkg.meshgen.config2(ne=sample_ne)
+    q = pkg.meshgen.jittered_cube(ne=sample_ne)
     t0 = time.perf_counter()
     K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3, nthreads=threads)
     t_asm = time.perf_counter() - t0
@@ -240,7 +240,7 @@ def reference_arm(args, dist):
     from oracle import coracle
     coracle.build()
     sample_ne = min(64, ne)
-    q = pkg.meshgen.config2(ne=sample_ne)
+    q = pkg.meshgen.jittered_cube(ne=sample_ne)
     Kq = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3,
                           nthreads=coracle.max_threads())
     _, st = Kq.solve(q.fixed_dofs, q.fixed_vals, rtol=args.rtol, nthreads=coracle.max_threads())
@@ -286,7 +286,7 @@ def our_arm(args, dist):
     ctx = pkg.get_context(dev_index)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
 
-    p = pkg.meshgen.config2(ne=args.ne)
+    p = pkg.meshgen.jittered_cube(ne=args.ne)
     nN, nEl = p.n_nodes, p.n_elem
     n_dof = p.n_dof
     NLf = np.asfortranarray(p.NodeList)
@@ -367,8 +367,8 @@ def our_arm(args, dist):
         fp64_peak, fp32_peak = probe_fp64_peak(dev_index)
         line.update({
             "value": value, "ms_per_step": ms,
-            "config": {"workload": f"{args.ne}^3 Q1 hex elasticity (configs[1]): FP64 assembly + "
-                                   f"Jacobi-PCG to {args.rtol:g}",
+            "config": {"workload": f"{args.ne}^3 jittered Q1 hex elasticity, E ~ lognormal(0, 0.5): FP64 "
+                                   f"assembly + Jacobi-PCG to {args.rtol:g}",
                        "ne": args.ne, "n_dof": n_dof, "nnz": nnz, "precision": "fp64", "precond": "jacobi",
                        "rtol": args.rtol, "parallelism": f"replicas x{dist.world}",
                        "l2": "inputs larger than L2 (K alone is %.1f GB), no flush" % (nnz * 8 / 1e9)},
@@ -453,7 +453,7 @@ def precision_leg(args, pkg, ctx, stream, dist):
     with FP64 residual refreshes, both to 1e-10 relative residual; the mixed
     result's error is measured against a tight FP64 solve (1e-13)."""
     import torch
-    p = pkg.meshgen.config3(ne=args.precision_ne)
+    p = pkg.meshgen.contrast_cube(ne=args.precision_ne)
     dev = torch.device("cuda", ctx.device)
     NLf, IENf, IDf = (np.asfortranarray(a) for a in (p.NodeList, p.IEN, p.ID))
     dX = torch.from_numpy(NLf.ravel(order="F")).to(dev)
@@ -497,8 +497,8 @@ def precision_leg(args, pkg, ctx, stream, dist):
 
     fp64 = run("fp64", "jacobi")
     mixed = run("mixed", "block_jacobi")
-    return {"workload": f"{p.ne}^3 Q1 hex elasticity, E ~ lognormal(0, 1), nu ~ U(0.25, 0.45) per element "
-                        "(configs[2]); assemble + Dirichlet + PCG to 1e-10, inputs on the device",
+    return {"workload": f"{p.ne}^3 Q1 hex elasticity, E ~ lognormal(0, 1), nu ~ U(0.25, 0.45) per element; "
+                        "assemble + Dirichlet + PCG to 1e-10, inputs on the device",
             "n_dof": p.n_dof, "fp64_jacobi": fp64, "mixed_block_jacobi": mixed,
             "speedup_mixed_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
             "rel_err_reference": "FP64 Jacobi-PCG on the GPU to relative residual 1e-13"}
@@ -511,7 +511,7 @@ def batch_leg(args, pkg, ctx, stream, dist):
     Beside it: the plain FP64 GPU path (single-mesh API, Jacobi-PCG, one mesh
     after another) on the same meshes."""
     import torch
-    probs = pkg.meshgen.config4(count=args.batch_count)
+    probs = pkg.meshgen.quad_batch(count=args.batch_count)
     n_total = int(sum(p.n_dof for p in probs))
     nus = np.array([float(p.nu[0]) for p in probs])
     fixed = [p.fixed_dofs for p in probs]
@@ -649,7 +649,7 @@ def serve_leg(args, pkg, ctx, dist):
     mesh size, mixed-precision block-Jacobi PCG.  Requests draw from a pool
     of distinct meshes, so a repeated request must give the same bits."""
     rng = np.random.default_rng(2005)
-    pool = [p for _, p in pkg.meshgen.config5_stream(args.serve_pool)]
+    pool = [p for _, p in pkg.meshgen.serving_stream(args.serve_pool)]
     rtol = args.batch_rtol
     # the whole GPU for the kernel: after the warm-up every topology is cached, so
     # no pattern build needs free SMs during the measured streams

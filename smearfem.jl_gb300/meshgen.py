@@ -9,7 +9,7 @@ arrays have the reference's shapes: ``NodeList`` (ndim, nN), ``IEN`` (nEl, nen),
 ``ID`` (nN, ndim).
 
 The workload builders produce the seeded inputs of the five benchmark
-configurations (20^3 unit-cube parity case, 128^3 jittered FP64 case, 96^3
+workloads (20^3 unit-cube parity case, 128^3 jittered FP64 case, 96^3
 high-contrast mixed-precision case, 1024-mesh plane-strain batch, serving
 stream).  Every random draw comes from ``numpy.random.default_rng(seed)``.
 Boundary nodes are never jittered, so face selection by exact coordinate
@@ -211,29 +211,29 @@ def squeeze_problem(ne=8, Young=40.0, nu=0.4):
 
 # ---- the five benchmark workloads ------------------------------------------
 
-def config1():
+def parity_cube20():
     """20^3 unit cube, E=1, nu=0.3, no jitter, u_z = 0.05 sin(pi x) sin(pi y) on top."""
     return hex_problem(20, 1001, jitter=0.0, top="sin", rtol=1e-12, name="cube20")
 
 
-def config2(ne=128):
+def jittered_cube(ne=128):
     """128^3 jittered (0.2h) cube, E ~ lognormal(0, 0.5), nu=0.3, 4-mode top load, FP64 PCG 1e-10."""
     return hex_problem(ne, 1002, jitter=0.2, e_sigma=0.5, nu=0.3, top="modes",
                        rtol=1e-10, name=f"cube{ne}_jit")
 
 
-def config3(ne=96):
+def contrast_cube(ne=96):
     """96^3 jittered cube, E ~ lognormal(0, 1), nu ~ U(0.25, 0.45), 4-mode top load."""
     return hex_problem(ne, 1003, jitter=0.2, e_sigma=1.0, nu_range=(0.25, 0.45),
                        top="modes", rtol=1e-10, name=f"cube{ne}_contrast")
 
 
-def config4_sizes(count=1024, seed=1004, lo=16, hi=256):
+def quad_batch_sizes(count=1024, seed=1004, lo=16, hi=256):
     rng = np.random.default_rng(seed)
     return rng.integers(lo, hi + 1, count)
 
 
-def config4(count=1024, seed=1004, lo=16, hi=256):
+def quad_batch(count=1024, seed=1004, lo=16, hi=256):
     """``count`` plane-strain unit squares, n ~ U{lo..hi}, jitter 0.15h, E=1, nu_mesh ~ U(0.2, 0.45)."""
     rng = np.random.default_rng(seed)
     sizes = rng.integers(lo, hi + 1, count)
@@ -242,7 +242,7 @@ def config4(count=1024, seed=1004, lo=16, hi=256):
             for b, n in enumerate(sizes)]
 
 
-def config5_stream(count, seed=1005, rate=2000.0, lo2=32, hi2=512, lo3=16, hi3=64):
+def serving_stream(count, seed=1005, rate=2000.0, lo2=32, hi2=512, lo3=16, hi3=64):
     """Serving stream: Poisson arrivals at ``rate``/s; 70% 2D quads, 30% 3D hexes.
 
     Yields ``(arrival_s, Problem)``; E ~ lognormal(0, 0.5) per element,

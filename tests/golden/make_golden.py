@@ -71,7 +71,7 @@ def make_small():
 
 
 def make_cube20():
-    p = M.config1()
+    p = M.parity_cube20()
     K = R.assemble_system(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, 1.0, 0.3)
     u = R.solve_eliminated(K, p.fixed_dofs, p.fixed_vals, method="inv")
     colptr, rowval, nzval, m, n = K

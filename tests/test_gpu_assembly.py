@@ -81,7 +81,7 @@ def test_assembly_vs_oracle(sfem, ctx, oracle, case):
 
 def test_cube20_vs_c_oracle(sfem, ctx, coracle):
     """The 20^3 unit cube (27,783 DOFs, 2,042,829 nonzeros)."""
-    p = sfem.meshgen.config1()
+    p = sfem.meshgen.parity_cube20()
     ref = coracle.assemble(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, 1.0, 0.3, nthreads=0).arrays()
     got = _assemble(sfem, ctx, p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, 1.0, 0.3)
     assert len(got[1][2]) == 2042829
@@ -90,7 +90,7 @@ def test_cube20_vs_c_oracle(sfem, ctx, coracle):
 
 def test_jittered_lognormal_vs_c_oracle(sfem, ctx, coracle):
     """A reduced copy of the 128^3 benchmark mesh: 16^3, jitter 0.2h, E ~ lognormal(0, 0.5)."""
-    p = sfem.meshgen.config2(ne=16)
+    p = sfem.meshgen.jittered_cube(ne=16)
     ref = coracle.assemble(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, p.Young, 0.3).arrays()
     got = _assemble(sfem, ctx, p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, p.Young, 0.3)
     _check(None, ref, got)
@@ -142,7 +142,7 @@ def test_general_id_and_unused_nodes(sfem, ctx, oracle):
 
 
 def test_deterministic_and_symmetric(sfem, ctx):
-    p = sfem.meshgen.config2(ne=12)
+    p = sfem.meshgen.jittered_cube(ne=12)
     a = _assemble(sfem, ctx, p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, p.Young, 0.3)[1]
     b = _assemble(sfem, ctx, p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, p.Young, 0.3)[1]
     for x, y in zip(a, b):
@@ -157,7 +157,7 @@ def test_deterministic_and_symmetric(sfem, ctx):
 def test_large_mesh_properties(sfem, ctx):
     """48^3 hex (352,947 DOFs): nnz formula, rigid-body null space, symmetry."""
     ne = 48
-    p = sfem.meshgen.config2(ne=ne)
+    p = sfem.meshgen.jittered_cube(ne=ne)
     K = sfem.assemble_system(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, p.Young, 0.3, ctx=ctx)
     assert K.nnz == 9 * (3 * (ne + 1) - 2) ** 3
     X = p.NodeList

@@ -31,7 +31,7 @@ def _handle(sfem, ctx, p):
 def test_cube20_vs_dense_inverse(sfem, ctx, precision, precond):
     """20^3 unit cube vs the reference's own algorithm: dense inverse of K_free."""
     g = np.load(GOLDEN)
-    p = sfem.meshgen.config1()
+    p = sfem.meshgen.parity_cube20()
     K = _handle(sfem, ctx, p)
     assert K.n == int(g["n"]) and K.nnz == int(g["nnz"])
     u, st = K.solve(p.fixed_dofs, p.fixed_vals, precision=precision, precond=precond, rtol=1e-12)
@@ -95,7 +95,7 @@ def test_patch_test_linear_field(sfem, ctx):
 
 def test_medium_vs_c_oracle(sfem, ctx, coracle):
     """24^3 jittered lognormal mesh (46,875 DOFs) vs the C oracle's FP64 PCG at 1e-13."""
-    p = sfem.meshgen.config2(ne=24)
+    p = sfem.meshgen.jittered_cube(ne=24)
     Kc = coracle.assemble(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, p.Young, 0.3)
     uref, _ = Kc.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13)
     K = _handle(sfem, ctx, p)
@@ -127,7 +127,7 @@ def test_solver_status_paths(sfem, ctx):
 
 
 def test_repeatable_bitwise(sfem, ctx):
-    p = sfem.meshgen.config2(ne=10)
+    p = sfem.meshgen.jittered_cube(ne=10)
     K = _handle(sfem, ctx, p)
     for precision in ("fp64", "mixed"):
         a, _ = K.solve(p.fixed_dofs, p.fixed_vals, precision=precision)
@@ -140,7 +140,7 @@ def test_repeatable_bitwise(sfem, ctx):
 def test_mixed_fp32_storages(sfem, ctx, storage, precond):
     """The mixed solver's FP32 K as upper-triangle blocks (default) or full
     blocks: both reach the FP64 solution within 1e-8."""
-    p = sfem.meshgen.config3(ne=12)
+    p = sfem.meshgen.contrast_cube(ne=12)
     K = _handle(sfem, ctx, p)
     ref, _ = K.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13)
     u, st = K.solve(p.fixed_dofs, p.fixed_vals, precision="mixed", precond=precond, rtol=1e-11,

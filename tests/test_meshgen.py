@@ -13,7 +13,7 @@ def test_meshgrid_matches_loop_restatement(sfem, oracle, ndim, ne):
 
 
 def test_workloads_are_seeded_and_valid(sfem, oracle):
-    for make in (lambda: sfem.meshgen.config2(ne=8), lambda: sfem.meshgen.config3(ne=8)):
+    for make in (lambda: sfem.meshgen.jittered_cube(ne=8), lambda: sfem.meshgen.contrast_cube(ne=8)):
         p, q = make(), make()
         assert np.array_equal(p.NodeList, q.NodeList) and np.array_equal(p.Young, q.Young)
         assert np.array_equal(p.fixed_vals, q.fixed_vals)
@@ -29,8 +29,8 @@ def test_workloads_are_seeded_and_valid(sfem, oracle):
         assert np.unique(p.fixed_dofs).size == p.fixed_dofs.size
 
 
-def test_config1_sizes(sfem):
-    p = sfem.meshgen.config1()
+def test_parity_cube20_sizes(sfem):
+    p = sfem.meshgen.parity_cube20()
     assert p.n_nodes == 9261 and p.n_dof == 27783
     # bottom face: 441 nodes x 3 DOFs; top face: 441 z-DOFs
     assert p.fixed_dofs.size == 441 * 3 + 441
@@ -38,11 +38,11 @@ def test_config1_sizes(sfem):
 
 
 def test_batch_and_stream_generators(sfem):
-    sizes = sfem.meshgen.config4_sizes()
+    sizes = sfem.meshgen.quad_batch_sizes()
     assert sizes.size == 1024 and sizes.min() >= 16 and sizes.max() <= 256
-    batch = sfem.meshgen.config4(count=4)
+    batch = sfem.meshgen.quad_batch(count=4)
     assert all(p.plane == "strain" and p.ndim == 2 for p in batch)
-    stream = list(sfem.meshgen.config5_stream(20))
+    stream = list(sfem.meshgen.serving_stream(20))
     t = [a for a, _ in stream]
     assert all(b > a for a, b in zip(t, t[1:]))
     assert {p.ndim for _, p in stream} <= {2, 3}

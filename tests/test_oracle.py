@@ -207,7 +207,7 @@ def test_cube20_fixture_matches_c_oracle(coracle, meshgen):
     """The committed dense-inverse displacement of the 20^3 cube agrees with
     the C oracle's PCG, and the checksums of K match."""
     g = np.load(os.path.join(GOLDEN_DIR, "cube20_dense_inv.npz"))
-    p = meshgen.config1()
+    p = meshgen.parity_cube20()
     K = coracle.assemble(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, 1.0, 0.3)
     colptr, rowval, nzval, m, n = K.arrays()
     assert n == int(g["n"]) and len(nzval) == int(g["nnz"])

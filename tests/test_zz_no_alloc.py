@@ -36,7 +36,7 @@ def _noalloc(sfem, ctx, K, young, nu):
 
 
 def test_noalloc_matches_assemble_twice(sfem, ctx):
-    p = sfem.meshgen.config2(ne=14)                      # 2,744 hex elements: fits the 64 MiB array
+    p = sfem.meshgen.jittered_cube(ne=14)                      # 2,744 hex elements: fits the 64 MiB array
     m = sfem.Mesh(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, ctx=ctx)
     rng = np.random.default_rng(77)
     mats = [(p.Young, 0.3), (np.exp(rng.normal(0, 1.0, p.n_elem)), rng.uniform(0.25, 0.45, p.n_elem))]
@@ -71,7 +71,7 @@ def test_noalloc_scalar_and_fp32_copy(sfem, ctx):
 
 
 def test_noalloc_refuses_meshes_beyond_its_scratch(sfem, ctx):
-    p = sfem.meshgen.config2(ne=30)                      # 27,000 hex elements > 64 MiB of blocks
+    p = sfem.meshgen.jittered_cube(ne=30)                      # 27,000 hex elements > 64 MiB of blocks
     m = sfem.Mesh(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, ctx=ctx)
     K = m.assemble(p.Young, 0.3)
     assert _noalloc(sfem, ctx, K, p.Young, 0.3) == 1     # SFEM_BAD_ARG
