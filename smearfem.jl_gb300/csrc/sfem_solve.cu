@@ -194,16 +194,18 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
         // upper and lower parts in one loop: the lower part's loads depend on
         // its index entry, the upper part's do not, so interleaving them keeps
         // more independent loads in flight; the next index entry is prefetched.
+        // Index arrays are read once (streaming hint); the upper values are read
+        // again as a neighbour's lower blocks, so they keep the normal policy.
         const int64_t u0 = sptrU[s], nu = sptrU[s + 1] - u0;
         const int64_t l0 = sptrL[s], nl = sptrL[s + 1] - l0;
         const int64_t nk = nu > nl ? nu : nl;
-        int2 ent_next = nl > 0 ? __ldg(&lo[l0 * 32 + lane]) : make_int2(-1, 0);
+        int2 ent_next = nl > 0 ? __ldcs(&lo[l0 * 32 + lane]) : make_int2(-1, 0);
         for (int64_t k = 0; k < nk; ++k) {
             const int2 ent = ent_next;
-            if (k + 1 < nl) ent_next = __ldg(&lo[(l0 + k + 1) * 32 + lane]);
+            if (k + 1 < nl) ent_next = __ldcs(&lo[(l0 + k + 1) * 32 + lane]);
             if (k < nu) {
                 const int64_t su = u0 + k;
-                const int c = __ldg(&colU[su * 32 + lane]);
+                const int c = __ldcs(&colU[su * 32 + lane]);
                 T v[B * B];
 #pragma unroll
                 for (int e = 0; e < B * B; ++e) v[e] = __ldg(&valU[(su * B * B + e) * 32 + lane]);
