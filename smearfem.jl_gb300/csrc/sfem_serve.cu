@@ -266,8 +266,8 @@ struct Request {
     bool finished = false;
     int status = SFEM_OK;
     std::vector<double> u;
-    sfem_batch_stats stats;
-    ServeTrace trace;
+    sfem_batch_stats stats{};
+    ServeTrace trace{};
     std::chrono::steady_clock::time_point t_submit, t_publish, t_done;
 };
 
@@ -397,11 +397,13 @@ int start_kernel(sfem_server *s) {
 void release_request_buffers(sfem_server *s, Request *r) {
     for (void *p : r->bufs) sfem_dfree(s->ctx, p);
     r->bufs.clear();
-    if (r->key == 0) {
-        if (r->mesh) sfem_mesh_release(r->mesh);
-    } else {
-        auto it = s->topo.find(r->key);
-        if (it != s->topo.end()) it->second.refs--;
+    if (r->mesh) {  // set only once the request holds its pattern (own, or a counted reference)
+        if (r->key == 0) {
+            sfem_mesh_release(r->mesh);
+        } else {
+            auto it = s->topo.find(r->key);
+            if (it != s->topo.end()) it->second.refs--;
+        }
     }
     r->mesh = nullptr;
 }

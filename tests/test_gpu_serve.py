@@ -146,6 +146,42 @@ def test_3d_hex_and_scalar_requests(sfem, ctx):
 
 
 @pytest.mark.timeout(300)
+def test_scalar_classes_3d_and_q2(sfem, ctx):
+    """The scalar branches of the serving kernel: 3D Q1 and 2D Q2 Laplace."""
+    mg = sfem.meshgen
+    cases = []
+    NL, IEN, _, _, _ = mg.meshgrid(0, 1, 0, 1, 0, 1, 5, 3)
+    bnd = np.flatnonzero(np.any((NL == 0) | (NL == 1), axis=0)) + 1
+    cases.append((NL, IEN, 3, "Q1", bnd, NL[0, bnd - 1] * NL[1, bnd - 1] + NL[2, bnd - 1], 5))
+    # 2D Q2: 9-node elements on a (2n+1)^2 node grid
+    n = 4
+    m1 = 2 * n + 1
+    xs = np.linspace(0, 1, m1)
+    X, Y = np.meshgrid(xs, xs, indexing="xy")
+    NL2 = np.stack([X.ravel(), Y.ravel()])
+    rows = []
+    for j in range(n):
+        for i in range(n):
+            b0 = 2 * j * m1 + 2 * i + 1
+            c = [b0, b0 + 2, b0 + 2 * m1 + 2, b0 + 2 * m1, b0 + 1, b0 + m1 + 2, b0 + 2 * m1 + 1, b0 + m1,
+                 b0 + m1 + 1]
+            rows.append(c)
+    IEN2 = np.array(rows, dtype=np.int64)
+    bnd2 = np.flatnonzero(np.any((NL2 == 0) | (NL2 == 1), axis=0)) + 1
+    cases.append((NL2, IEN2, 2, "Q2", bnd2, np.cos(2 * NL2[0, bnd2 - 1]) + NL2[1, bnd2 - 1] ** 2, n))
+    with sfem.Server(cluster=2, rtol=1e-12) as srv:
+        ids = [srv.submit(NLc, IENc, None, 1.0, 0.3, b_, v_, ndim=nd, nDof=1, FunctionClass=fc)
+               for NLc, IENc, nd, fc, b_, v_, _ in cases]
+        outs = [srv.wait(i, timeout_ms=60000) for i in ids]
+    for (NLc, IENc, nd, fc, b_, v_, ne), (u, res) in zip(cases, outs):
+        assert res["status"] == 0
+        K = sfem.assemble_system(ne, NLc, IENc, nd, fc, 1, ctx=ctx, as_handle=True)
+        ref = K.solve(b_, v_, rtol=1e-13)[0]
+        K.close()
+        assert _rel(u, ref) <= TOL_U, fc
+
+
+@pytest.mark.timeout(300)
 def test_mixed_classes_in_one_stream(sfem, ctx):
     """2D and 3D requests interleaved on one server, each matching its own solve."""
     mg = sfem.meshgen
