@@ -375,6 +375,21 @@ __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr,
     return dot;
 }
 
+// grp_spmv as a separate function: a kernel that inlines several element
+// classes' pipelines allocates registers for all of them at once, and the
+// CG's SpMV of one class can come out slower there than on its own.  Called
+// once per CG iteration, the call costs nothing measurable and the SpMV keeps
+// the register allocation it gets in a single-class kernel.
+template <typename T, int B, bool FUSE_P, int U, int W>
+__device__ __noinline__ double grp_spmv_call(const int64_t *__restrict__ sliceptr, const int *__restrict__ col,
+                                             const T *__restrict__ val, int64_t sfirst, int64_t s1, int64_t sstride,
+                                             int64_t rend, const T *__restrict__ x, const T *__restrict__ z, T beta,
+                                             T *__restrict__ pnew, T *__restrict__ y,
+                                             const unsigned char *__restrict__ fixed, bool masked) {
+    return grp_spmv<T, B, FUSE_P, U, W>(sliceptr, col, val, sfirst, s1, sstride, rend, x, z, beta, pnew, y, fixed,
+                                        masked);
+}
+
 // One CTA working alone on a mesh.
 struct SoloGroup {
     __device__ __forceinline__ int rank() const { return 0; }
@@ -428,7 +443,8 @@ struct ClusterGroup {
 // UF: slabs in flight per thread in the CG loop's SpMV, WF: slice width of
 // its pipelined path (0: none), NV: nodes per thread and step of the vector
 // update.  The register budget of the calling kernel decides what fits.
-template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF = 4, int WF = 0, int NVF = 1>
+template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF = 4, int WF = 0, int NVF = 1,
+          bool SPMV_CALL = false>
 __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
                              int *s_flag) {
     using T = typename std::conditional<MIXED, float, double>::type;
@@ -782,9 +798,14 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
         bool done = status != SFEM_OK || !(bb > 0.0);
         while (!done) {
             // q = K p with p = z + beta p_prev formed inside the SpMV (stored to pw)
-            double pq = grp_spmv<T, B, true, (sizeof(T) == 8 ? 2 : UF), (sizeof(T) == 8 ? 0 : WF)>(
-                a.sliceptr, a.col, valT, M.slice0 + gw, M.slice1, gnw, n1, pv, zv,
-                                             (T)beta, pw, qv, a.fixed, true);
+            constexpr int US = sizeof(T) == 8 ? 2 : UF, WS = sizeof(T) == 8 ? 0 : WF;
+            double pq;
+            if constexpr (SPMV_CALL)
+                pq = grp_spmv_call<T, B, true, US, WS>(a.sliceptr, a.col, valT, M.slice0 + gw, M.slice1, gnw, n1, pv,
+                                                       zv, (T)beta, pw, qv, a.fixed, true);
+            else
+                pq = grp_spmv<T, B, true, US, WS>(a.sliceptr, a.col, valT, M.slice0 + gw, M.slice1, gnw, n1, pv, zv,
+                                                  (T)beta, pw, qv, a.fixed, true);
             {
                 T *t = pv;  // pv: the current direction
                 pv = pw;
