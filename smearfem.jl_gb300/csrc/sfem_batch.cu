@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
     __shared__ double xch[4];
     __shared__ int s_flag, s_mesh;
     constexpr int WF = (NDIM == 2 && NEN == 4 && B == 2) ? 9 : 0;  // pipelined 9-slab slices of 2D Q1 elasticity
+    constexpr int UF = (NDIM == 3 && B == 3) ? 9 : 4;                 // 3D elasticity: 9 slabs in flight
     const int tid = threadIdx.x;
     cgrp::cluster_group cl = cgrp::this_cluster();
     // 1. large meshes: the whole cluster works on one mesh
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = *cl.map_shared_rank(&s_mesh, 0);
         cl.sync();
         if (q >= a.nbig) break;
-        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED, 4, WF>(ClusterGroup(), tab, a, a.order[q], red, xch, &s_flag);
+        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED, UF, WF>(ClusterGroup(), tab, a, a.order[q], red, xch, &s_flag);
         cl.sync();
     }
     // 2. small meshes: every CTA on its own
@@ -83,7 +84,7 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = (int64_t)a.nbig + s_mesh;
         __syncthreads();
         if (q >= a.nmesh) break;
-        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED, 4, WF>(SoloGroup(), tab, a, a.order[q], red, xch, &s_flag);
+        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED, UF, WF>(SoloGroup(), tab, a, a.order[q], red, xch, &s_flag);
         __syncthreads();
     }
     cl.sync();  // peers may still read this CTA's shared memory until every CTA is done
