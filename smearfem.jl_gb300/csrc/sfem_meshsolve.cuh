@@ -390,6 +390,91 @@ __device__ __noinline__ double grp_spmv_call(const int64_t *__restrict__ slicept
                                         masked);
 }
 
+// The CG vector update of one group's nodes: x += alpha p, r -= alpha q,
+// z = M^-1 r, and this thread's shares of r.z and r.r.
+template <typename T, int B, int NVF>
+__device__ __forceinline__ double2 cg_update(T *__restrict__ xv, T *__restrict__ rv, T *__restrict__ zv,
+                                             const T *__restrict__ pv, const T *__restrict__ qv,
+                                             const T *__restrict__ minv, T alpha, int64_t n0, int64_t n1, int64_t gt,
+                                             int64_t gstride) {
+    double prz = 0.0, prr = 0.0;
+    // x += alpha p, r -= alpha q, z = M^-1 r; NV nodes per thread per step (loads first)
+    constexpr int NV = sizeof(T) == 8 ? 1 : NVF;
+    for (int64_t nb = n0 + gt; nb < n1; nb += NV * gstride) {
+        T P[NV][B], X[NV][B], Q[NV][B], R[NV][B], Mi[NV][B * B];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            const int64_t node = nb + v * gstride;
+            if (node < n1) {
+                if constexpr (sizeof(T) == 4 && B == 2) {  // one vector load per array
+                    const float2 p2 = *reinterpret_cast<const float2 *>(pv + node * 2);
+                    const float2 x2 = *reinterpret_cast<const float2 *>(xv + node * 2);
+                    const float2 q2 = *reinterpret_cast<const float2 *>(qv + node * 2);
+                    const float2 r2 = *reinterpret_cast<const float2 *>(rv + node * 2);
+                    const float4 m4 = *reinterpret_cast<const float4 *>(minv + node * 4);
+                    P[v][0] = p2.x, P[v][1] = p2.y, X[v][0] = x2.x, X[v][1] = x2.y;
+                    Q[v][0] = q2.x, Q[v][1] = q2.y, R[v][0] = r2.x, R[v][1] = r2.y;
+                    Mi[v][0] = m4.x, Mi[v][1] = m4.y, Mi[v][2] = m4.z, Mi[v][3] = m4.w;
+                } else {
+#pragma unroll
+                    for (int i = 0; i < B; ++i) {
+                        const int64_t d = node * B + i;
+                        P[v][i] = pv[d];
+                        X[v][i] = xv[d];
+                        Q[v][i] = qv[d];
+                        R[v][i] = rv[d];
+                    }
+#pragma unroll
+                    for (int e = 0; e < B * B; ++e) Mi[v][e] = minv[node * B * B + e];
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            const int64_t node = nb + v * gstride;
+            if (node < n1) {
+                T Xn[B], Z[B];
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    Xn[i] = fma(alpha, P[v][i], X[v][i]);
+                    R[v][i] = fma(-alpha, Q[v][i], R[v][i]);
+                    prr += (double)(R[v][i] * R[v][i]);
+                }
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    T zi = T(0);
+#pragma unroll
+                    for (int j = 0; j < B; ++j) zi = fma(Mi[v][i * B + j], R[v][j], zi);
+                    Z[i] = zi;
+                    prz += (double)(R[v][i] * zi);
+                }
+                if constexpr (sizeof(T) == 4 && B == 2) {
+                    *reinterpret_cast<float2 *>(xv + node * 2) = make_float2(Xn[0], Xn[1]);
+                    *reinterpret_cast<float2 *>(rv + node * 2) = make_float2(R[v][0], R[v][1]);
+                    *reinterpret_cast<float2 *>(zv + node * 2) = make_float2(Z[0], Z[1]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < B; ++i) {
+                        xv[node * B + i] = Xn[i];
+                        rv[node * B + i] = R[v][i];
+                        zv[node * B + i] = Z[i];
+                    }
+                }
+            }
+        }
+    }
+    return make_double2(prz, prr);
+}
+
+// cg_update as a separate function (see grp_spmv_call).
+template <typename T, int B, int NVF>
+__device__ __noinline__ double2 cg_update_call(T *__restrict__ xv, T *__restrict__ rv, T *__restrict__ zv,
+                                               const T *__restrict__ pv, const T *__restrict__ qv,
+                                               const T *__restrict__ minv, T alpha, int64_t n0, int64_t n1,
+                                               int64_t gt, int64_t gstride) {
+    return cg_update<T, B, NVF>(xv, rv, zv, pv, qv, minv, alpha, n0, n1, gt, gstride);
+}
+
 // One CTA working alone on a mesh.
 struct SoloGroup {
     __device__ __forceinline__ int rank() const { return 0; }
@@ -444,7 +529,7 @@ struct ClusterGroup {
 // its pipelined path (0: none), NV: nodes per thread and step of the vector
 // update.  The register budget of the calling kernel decides what fits.
 template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF = 4, int WF = 0, int NVF = 1,
-          bool SPMV_CALL = false>
+          bool SPMV_CALL = false, bool UPD_CALL = false>
 __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
                              int *s_flag) {
     using T = typename std::conditional<MIXED, float, double>::type;
@@ -817,71 +902,15 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                 break;
             }
             const T alpha = (T)(rz / pq);
-            double prz = 0.0, prr = 0.0;
-            // x += alpha p, r -= alpha q, z = M^-1 r; NV nodes per thread per step (loads first)
-            constexpr int NV = sizeof(T) == 8 ? 1 : NVF;
-            for (int64_t nb = n0 + gt; nb < n1; nb += NV * gstride) {
-                T P[NV][B], X[NV][B], Q[NV][B], R[NV][B], Mi[NV][B * B];
-#pragma unroll
-                for (int v = 0; v < NV; ++v) {
-                    const int64_t node = nb + v * gstride;
-                    if (node < n1) {
-                        if constexpr (sizeof(T) == 4 && B == 2) {  // one vector load per array
-                            const float2 p2 = *reinterpret_cast<const float2 *>(pv + node * 2);
-                            const float2 x2 = *reinterpret_cast<const float2 *>(xv + node * 2);
-                            const float2 q2 = *reinterpret_cast<const float2 *>(qv + node * 2);
-                            const float2 r2 = *reinterpret_cast<const float2 *>(rv + node * 2);
-                            const float4 m4 = *reinterpret_cast<const float4 *>(minv + node * 4);
-                            P[v][0] = p2.x, P[v][1] = p2.y, X[v][0] = x2.x, X[v][1] = x2.y;
-                            Q[v][0] = q2.x, Q[v][1] = q2.y, R[v][0] = r2.x, R[v][1] = r2.y;
-                            Mi[v][0] = m4.x, Mi[v][1] = m4.y, Mi[v][2] = m4.z, Mi[v][3] = m4.w;
-                        } else {
-#pragma unroll
-                            for (int i = 0; i < B; ++i) {
-                                const int64_t d = node * B + i;
-                                P[v][i] = pv[d];
-                                X[v][i] = xv[d];
-                                Q[v][i] = qv[d];
-                                R[v][i] = rv[d];
-                            }
-#pragma unroll
-                            for (int e = 0; e < B * B; ++e) Mi[v][e] = minv[node * B * B + e];
-                        }
-                    }
-                }
-#pragma unroll
-                for (int v = 0; v < NV; ++v) {
-                    const int64_t node = nb + v * gstride;
-                    if (node < n1) {
-                        T Xn[B], Z[B];
-#pragma unroll
-                        for (int i = 0; i < B; ++i) {
-                            Xn[i] = fma(alpha, P[v][i], X[v][i]);
-                            R[v][i] = fma(-alpha, Q[v][i], R[v][i]);
-                            prr += (double)(R[v][i] * R[v][i]);
-                        }
-#pragma unroll
-                        for (int i = 0; i < B; ++i) {
-                            T zi = T(0);
-#pragma unroll
-                            for (int j = 0; j < B; ++j) zi = fma(Mi[v][i * B + j], R[v][j], zi);
-                            Z[i] = zi;
-                            prz += (double)(R[v][i] * zi);
-                        }
-                        if constexpr (sizeof(T) == 4 && B == 2) {
-                            *reinterpret_cast<float2 *>(xv + node * 2) = make_float2(Xn[0], Xn[1]);
-                            *reinterpret_cast<float2 *>(rv + node * 2) = make_float2(R[v][0], R[v][1]);
-                            *reinterpret_cast<float2 *>(zv + node * 2) = make_float2(Z[0], Z[1]);
-                        } else {
-#pragma unroll
-                            for (int i = 0; i < B; ++i) {
-                                xv[node * B + i] = Xn[i];
-                                rv[node * B + i] = R[v][i];
-                                zv[node * B + i] = Z[i];
-                            }
-                        }
-                    }
-                }
+            double prz, prr;
+            {
+                double2 pr;
+                if constexpr (UPD_CALL)
+                    pr = cg_update_call<T, B, NVF>(xv, rv, zv, pv, qv, minv, alpha, n0, n1, gt, gstride);
+                else
+                    pr = cg_update<T, B, NVF>(xv, rv, zv, pv, qv, minv, alpha, n0, n1, gt, gstride);
+                prz = pr.x;
+                prr = pr.y;
             }
             const double2 t = G.sum2(prz, prr, red, xch, ph++);
             ++it;
