@@ -653,8 +653,9 @@ def serve_leg(args, pkg, ctx, dist):
     rtol = args.batch_rtol
     # the whole GPU for the kernel: after the warm-up every topology is cached, so
     # no pattern build needs free SMs during the measured streams
-    srv = pkg.Server(precision="mixed", precond="block_jacobi", rtol=rtol, cluster=4, sm_fraction=1.0,
-                     idle_exit_ms=200.0)
+    # 8-CTA clusters of 256 threads (two per SM): measured 5% above 4 x 512 on this stream
+    srv = pkg.Server(precision="mixed", precond="block_jacobi", rtol=rtol, cluster=8, threads=256,
+                     sm_fraction=1.0, idle_exit_ms=200.0)
     try:
         # warm-up: every pool mesh once (builds and caches each topology's pattern)
         recs, t_warm = _stream(srv, pool, np.zeros(len(pool)), np.arange(len(pool)))
