@@ -135,3 +135,54 @@ int sfem_gather_blocks(sfem_ctx *ctx, const sfem_mesh *m, const double *kbuf, do
 int sfem_sym_build(sfem_ctx *ctx, sfem_matrix *K);
 int sfem_sym_refresh_values(sfem_ctx *ctx, sfem_matrix *K);
 void sfem_sym_free(sfem_ctx *ctx, sfem_matrix *K);
+
+// Lane-contiguous FP32 block layout (the per-mesh pipeline's K copy and the
+// upper-triangle storage of the mixed solver).  Each lane's block entries of
+// a slab are contiguous -- chunks of four, then the rest -- so a lane reads
+// its block with one (B = 2) or three (B = 3) vector loads while the warp
+// still reads whole contiguous segments: B = 1 one float per lane; B = 2 a
+// float4; B = 3 a float4, a float4 and a float (1152 bytes per slab, no
+// padding).  Fewer load instructions per product than the entry-major
+// layout.  STREAM: read with the evict-first hint (values used once).
+template <int B>
+__device__ __forceinline__ int64_t v32_at(int64_t slab, int lane, int e) {
+    if constexpr (B == 1) {
+        return slab * 32 + lane;
+    } else if constexpr (B == 2) {
+        return (slab * 32 + lane) * 4 + e;
+    } else {
+        const int64_t base = slab * 288;
+        return e < 4 ? base + lane * 4 + e : (e < 8 ? base + 128 + lane * 4 + (e - 4) : base + 256 + lane);
+    }
+}
+
+template <typename V>
+__device__ __forceinline__ V sfem_ld(const V *p, bool stream) {
+    return stream ? __ldcs(p) : __ldg(p);
+}
+
+template <int B, bool STREAM>
+__device__ __forceinline__ void load_v32(const float *__restrict__ v, int64_t slab, int lane, float *out) {
+    if constexpr (B == 1) {
+        out[0] = sfem_ld(v + slab * 32 + lane, STREAM);
+    } else if constexpr (B == 2) {
+        const float4 t = sfem_ld(reinterpret_cast<const float4 *>(v + (slab * 32 + lane) * 4), STREAM);
+        out[0] = t.x;
+        out[1] = t.y;
+        out[2] = t.z;
+        out[3] = t.w;
+    } else {
+        const float *b = v + slab * 288;
+        const float4 t0 = sfem_ld(reinterpret_cast<const float4 *>(b + lane * 4), STREAM);
+        const float4 t1 = sfem_ld(reinterpret_cast<const float4 *>(b + 128 + lane * 4), STREAM);
+        out[0] = t0.x;
+        out[1] = t0.y;
+        out[2] = t0.z;
+        out[3] = t0.w;
+        out[4] = t1.x;
+        out[5] = t1.y;
+        out[6] = t1.z;
+        out[7] = t1.w;
+        out[8] = sfem_ld(b + 256 + lane, STREAM);
+    }
+}

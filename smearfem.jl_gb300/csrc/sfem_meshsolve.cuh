@@ -154,57 +154,12 @@ __device__ __forceinline__ double2 block_sum2(double a, double b, double *sh, in
     return make_double2(x, y);
 }
 
-// FP32 copy of K inside the per-mesh pipeline.  Each lane's block entries of
-// a slab are contiguous -- chunks of four, then the rest -- so a lane reads
-// its block with one (B = 2) or three (B = 3) vector loads while the warp
-// still reads whole contiguous segments: B = 1 one float per lane; B = 2 a
-// float4; B = 3 a float4, a float4 and a float (1152 bytes per slab, no
-// padding).  Fewer load instructions per product: the CG loop of one group
-// is bound by memory latency and load issue, not by bytes.
-template <int B>
-__device__ __forceinline__ int64_t v32_at(int64_t slab, int lane, int e) {
-    if constexpr (B == 1) {
-        return slab * 32 + lane;
-    } else if constexpr (B == 2) {
-        return (slab * 32 + lane) * 4 + e;
-    } else {
-        const int64_t base = slab * 288;
-        return e < 4 ? base + lane * 4 + e : (e < 8 ? base + 128 + lane * 4 + (e - 4) : base + 256 + lane);
-    }
-}
-
-template <int B>
-__device__ __forceinline__ void load_v32(const float *__restrict__ v, int64_t slab, int lane, float *out) {
-    if constexpr (B == 1) {
-        out[0] = __ldcs(v + slab * 32 + lane);
-    } else if constexpr (B == 2) {
-        const float4 t = __ldcs(reinterpret_cast<const float4 *>(v + (slab * 32 + lane) * 4));
-        out[0] = t.x;
-        out[1] = t.y;
-        out[2] = t.z;
-        out[3] = t.w;
-    } else {
-        const float *b = v + slab * 288;
-        const float4 t0 = __ldcs(reinterpret_cast<const float4 *>(b + lane * 4));
-        const float4 t1 = __ldcs(reinterpret_cast<const float4 *>(b + 128 + lane * 4));
-        out[0] = t0.x;
-        out[1] = t0.y;
-        out[2] = t0.z;
-        out[3] = t0.w;
-        out[4] = t1.x;
-        out[5] = t1.y;
-        out[6] = t1.z;
-        out[7] = t1.w;
-        out[8] = __ldcs(b + 256 + lane);
-    }
-}
-
 // Block of K at (slab, lane): FP32 from the per-mesh layout above, FP64 from
 // the sliced-ELL layout (entry-major).
 template <typename T, int B>
 __device__ __forceinline__ void load_block(const T *__restrict__ val, int64_t slab, int lane, T *out) {
     if constexpr (sizeof(T) == 4) {
-        load_v32<B>(val, slab, lane, out);
+        load_v32<B, true>(val, slab, lane, out);
     } else {
 #pragma unroll
         for (int e = 0; e < B * B; ++e) out[e] = __ldcs(val + (slab * B * B + e) * 32 + lane);

@@ -207,8 +207,7 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
                 const int64_t su = u0 + k;
                 const int c = __ldcs(&colU[su * 32 + lane]);
                 T v[B * B];
-#pragma unroll
-                for (int e = 0; e < B * B; ++e) v[e] = __ldg(&valU[(su * B * B + e) * 32 + lane]);
+                load_v32<B, false>(valU, su, lane, v);
                 T xc[B];
 #pragma unroll
                 for (int j = 0; j < B; ++j) xc[j] = __ldg(&x[(int64_t)c * B + j]);
@@ -220,8 +219,7 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
             if (k < nl && ent.x >= 0) {  // ent.x < 0: padding
                 const int c = ent.y;
                 T v[B * B];
-#pragma unroll
-                for (int e = 0; e < B * B; ++e) v[e] = __ldg(&valU[ent.x + e * 32]);
+                load_v32<B, false>(valU, ent.x >> 5, ent.x & 31, v);
                 T xc[B];
 #pragma unroll
                 for (int j = 0; j < B; ++j) xc[j] = __ldg(&x[(int64_t)c * B + j]);

@@ -3,9 +3,10 @@
 // K is assembled bitwise symmetric (block(r,c) == block(c,r)^T), so the FP32
 // inner CG only needs, per node row r,
 //   upper part: the blocks (r, c) with c >= r, values stored, sliced-ELL:
-//       colU[slabU*32 + lane], valU[(slabU*b*b + i*b + j)*32 + lane]
+//       colU[slabU*32 + lane], valU in the lane-contiguous block layout
+//       (v32_at: each lane's block is one float4 + float4 + float for b = 3)
 //   lower part: for every neighbour c < r, where block (c, r) sits in c's
-//       upper part, as int2 {offset of its first value in valU, c}:
+//       upper part, as int2 {slabU*32 + lane of that block, c}:
 //       lo[slabL*32 + lane]   ({-1, 0} = padding).  Both are in one 8-byte
 //       load, so the value and x loads issue together (no dependent lookup).
 // y_r = sum_{c>=r} A_rc x_c + sum_{c<r} A_cr^T x_c, computed by one lane per
@@ -73,7 +74,7 @@ __global__ void k_sym_fill_upper(const int64_t *__restrict__ sliceptr, const int
         if (colU) colU[su * 32 + lane] = live ? col[(slab0 + kd + k) * 32 + lane] : (r < nN ? (int)r : 0);
 #pragma unroll
         for (int e = 0; e < B * B; ++e)
-            valU[(su * B * B + e) * 32 + lane] = live ? (float)val[((slab0 + kd + k) * B * B + e) * 32 + lane] : 0.0f;
+            valU[v32_at<B>(su, lane, e)] = live ? (float)val[((slab0 + kd + k) * B * B + e) * 32 + lane] : 0.0f;
     }
 }
 
@@ -109,7 +110,7 @@ __global__ void k_sym_fill_lower(const int64_t *__restrict__ sliceptr, const int
                 if (v < r) lo_i = mid + 1;
                 else hi_i = mid - 1;
             }
-            const int64_t off = ((sptrU[c >> 5] + (pos - ckd)) * B * B) * 32 + cl;
+            const int64_t off = (sptrU[c >> 5] + (pos - ckd)) * 32 + cl;  // slab and lane of block (c, r)
             if (pos < 0 || off > (int64_t)INT_MAX) {
                 atomicExch(bad, 1);
             } else {
