@@ -40,7 +40,6 @@ namespace {
 
 constexpr int SPMV_T = 256;
 constexpr int UPD_T = 256;
-constexpr int UPD_NODES = 128;  // nodes per CTA of k_update (B * 128 threads)
 
 struct CgScalars {
     double rz, rz_prev, pAp, alpha, beta, rr, bb, tol2, rr_ref, delta2;
@@ -259,76 +258,10 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
 // MIXED: the recursive FP32 residual never ends the solve; reaching the
 // tolerance, dropping by delta since the last refresh, or hitting maxit
 // requests an FP64 refresh instead (k_fold / k_spmv MODE 2 / k_refresh).
-template <typename T, int B, int PC, bool MIXED>
-__global__ void __launch_bounds__(UPD_NODES * B)
-k_update(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
-         const T *__restrict__ q, const T *__restrict__ minv, CgScalars *S, double *partial) {
-    if (S->done) return;
-    // one thread per DOF (coalesced vector traffic); a CTA walks tiles of
-    // UPD_NODES whole nodes, whose residuals are staged in shared memory for
-    // the nodal block-Jacobi product.  The grid is sized to what is resident,
-    // so each launch pays few per-CTA reductions.
-    __shared__ T rs[UPD_NODES * B];
-    const int64_t nd = nN * B;
-    const T alpha = (T)S->alpha;
-    double rz = 0.0, rr = 0.0;
-    const int64_t ntiles = sfem_cdiv(nN, UPD_NODES);
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {  // uniform trip count per CTA
-        const int64_t d = tile * (UPD_NODES * B) + threadIdx.x;
-        T rv = T(0);
-        if (d < nd) {
-            x[d] = fma(alpha, p[d], x[d]);
-            rv = fma(-alpha, q[d], r[d]);
-            r[d] = rv;
-        }
-        T zi = T(0);
-        if (PC == 0 || B == 1) {
-            if (d < nd) zi = minv[d] * rv;
-        } else {
-            __syncthreads();  // rs of the previous tile is no longer read
-            rs[threadIdx.x] = rv;
-            __syncthreads();
-            if (d < nd) {
-                const int nl = threadIdx.x / B;
-                const T *mrow = minv + d * B;  // row (node*B + i) of the node's block
-#pragma unroll
-                for (int j = 0; j < B; ++j) zi = fma(mrow[j], rs[nl * B + j], zi);
-            }
-        }
-        if (d < nd) {
-            z[d] = zi;
-            rz += (double)(rv * zi);
-            rr += (double)(rv * rv);
-        }
-    }
-    double trz, trr;
-    if (reduce2_last(rz, rr, partial, &S->ticket[1], &trz, &trr) && threadIdx.x == 0) {
-        S->rr = trr;
-        S->it += 1;
-        S->rz_prev = S->rz;
-        S->rz = trz;
-        S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
-        if (!(trr == trr)) {
-            S->done = 1;
-            S->status = SFEM_SINGULAR;
-        } else if (MIXED) {
-            if (S->it >= S->maxit) S->maxit_hit = 1;
-            if (trr <= S->tol2 || trr <= S->delta2 * S->rr_ref || S->maxit_hit) S->refresh = 1;
-        } else if (trr <= S->tol2) {
-            S->done = 1;
-            S->status = SFEM_OK;
-        } else if (S->it >= S->maxit) {
-            S->done = 1;
-            S->status = SFEM_NOT_CONVERGED;
-        }
-    }
-}
-
-// The same update with one thread per node: a thread loads its node's B
-// entries of x, p, q, r and its nodal inverse block, and keeps them in
-// registers -- no shared-memory staging and no barrier per tile, and B + B*B
-// loads in flight per thread.  A warp's loads still cover contiguous
-// segments (32 consecutive nodes).
+// One thread per node: a thread loads its node's B entries of x, p, q, r and
+// its nodal inverse, and keeps them in registers -- no shared-memory staging,
+// no barrier, B + B*B loads in flight per thread.  A warp's loads still cover
+// contiguous segments (32 consecutive nodes).
 template <typename T, int B, int PC, bool MIXED>
 __global__ void __launch_bounds__(UPD_T)
 k_update_node(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
@@ -729,7 +662,7 @@ class Solver {
     double *r0vec = nullptr;  // initial residual: bvec, or b - K x0 for a warm start
     CgScalars *S = nullptr;
     int64_t nd = 0;  // internal DOFs = nN * b
-    unsigned spmv_grid = 1, upd_grid = 1, vec_grid = 1, upd2_grid = 1;
+    unsigned spmv_grid = 1, upd_grid = 1, vec_grid = 1;
     cudaGraphExec_t gexec = nullptr;
     std::vector<cudaEvent_t> events;
     double ms_spmv = 0.0;
@@ -936,7 +869,6 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
     nd = m->nN * b;
     spmv_grid = (unsigned)sfem_cdiv(m->nslices * 32 > 0 ? m->nslices * 32 : 1, SPMV_T);
     upd_grid = (unsigned)sfem_cdiv(m->nN, UPD_T);
-    upd2_grid = (unsigned)sfem_cdiv(m->nN > 0 ? m->nN : 1, UPD_NODES);
     vec_grid = (unsigned)sfem_cdiv(nd, 256);
     const long long launches0 = ctx->launches;
 
@@ -949,7 +881,7 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
     SFEM_TRY(alloc(&x64, nd, "x"));
     SFEM_TRY(alloc(&ug, n, "u"));
     SFEM_TRY(alloc(&S, 1, "CG scalars"));
-    SFEM_TRY(alloc(&partial, 2 * (int64_t)std::max(std::max(spmv_grid, upd2_grid), std::max(upd_grid, vec_grid)),
+    SFEM_TRY(alloc(&partial, 2 * (int64_t)std::max(spmv_grid, std::max(upd_grid, vec_grid)),
                    "partials"));
     SFEM_TRY(alloc(&dfix, nfix, "fixed dofs"));
     SFEM_TRY(alloc(&dvals, nfix, "fixed values"));
