@@ -175,13 +175,18 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
 
 // The same product from the upper-triangle copy (sfem_sym.cu):
 // y_r = sum_{c>=r} A_rc x_c + sum_{c<r} A_cr^T x_c, one lane per row.
-template <typename T, int B, int MODE>
+// FUSE: the multiplied vector is the new CG direction p = z + beta x
+// (x = the previous direction), formed on the fly from the gathered entries;
+// each lane stores its own rows of p to pout.  This replaces the separate
+// direction update (one pass over three vectors per iteration).
+template <typename T, int B, int MODE, bool FUSE = false>
 __global__ void __launch_bounds__(SPMV_T)
 k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, const T *__restrict__ valU,
            const int64_t *__restrict__ sptrL, const int2 *__restrict__ lo, int64_t nN, int64_t nslices,
            const T *__restrict__ x, T *__restrict__ y, const unsigned char *__restrict__ fixed, CgScalars *S,
-           double *partial) {
+           double *partial, const T *__restrict__ z = nullptr, T *__restrict__ pout = nullptr) {
     if (MODE == 1 && S->done) return;
+    const T beta = FUSE ? (T)S->beta : T(0);
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     double dot = 0.0;
@@ -209,7 +214,10 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
                 load_v32<B, false>(valU, su, lane, v);
                 T xc[B];
 #pragma unroll
-                for (int j = 0; j < B; ++j) xc[j] = __ldg(&x[(int64_t)c * B + j]);
+                for (int j = 0; j < B; ++j) {
+                    xc[j] = __ldg(&x[(int64_t)c * B + j]);
+                    if (FUSE) xc[j] = fma(beta, xc[j], __ldg(&z[(int64_t)c * B + j]));
+                }
 #pragma unroll
                 for (int i = 0; i < B; ++i)
 #pragma unroll
@@ -221,7 +229,10 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
                 load_v32<B, false>(valU, ent.x >> 5, ent.x & 31, v);
                 T xc[B];
 #pragma unroll
-                for (int j = 0; j < B; ++j) xc[j] = __ldg(&x[(int64_t)c * B + j]);
+                for (int j = 0; j < B; ++j) {
+                    xc[j] = __ldg(&x[(int64_t)c * B + j]);
+                    if (FUSE) xc[j] = fma(beta, xc[j], __ldg(&z[(int64_t)c * B + j]));
+                }
 #pragma unroll
                 for (int i = 0; i < B; ++i)
 #pragma unroll
@@ -234,7 +245,12 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
                 const int64_t d = r * B + i;
                 const T out = fixed[d] ? T(0) : acc[i];
                 y[d] = out;
-                if (MODE == 1) dot += (double)(x[d] * out);
+                T pd = x[d];
+                if (FUSE) {
+                    pd = fma(beta, pd, z[d]);
+                    pout[d] = pd;
+                }
+                if (MODE == 1) dot += (double)(pd * out);
             }
         }
     }
@@ -680,11 +696,13 @@ void Solver::launch_spmv(const T *val, const T *x, T *y, bool fused) {
             if (fused) {
                 auto kern = k_spmv_sym<float, B, 1>;
                 kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
-                    K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial);
+                    K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial,
+                    nullptr, nullptr);
             } else {
                 auto kern = k_spmv_sym<float, B, 0>;
                 kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
-                    K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial);
+                    K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial,
+                    nullptr, nullptr);
             }
             SFEM_LAUNCHED(ctx);
             return;
@@ -716,16 +734,42 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
     CgScalars *h = (CgScalars *)ctx->h_small;
     const int chunk = opts.check_every > 0 ? opts.check_every : 32;
     const bool profile = opts.profile != 0;
+    // With the upper-triangle FP32 SpMV the direction update is folded into
+    // the SpMV, which writes p to the other of two buffers; an even chunk keeps
+    // the buffers' roles the same at every graph launch.
+    T *p2 = nullptr;
+    bool fuse_p = false;
+    if constexpr (sizeof(T) == 4) {
+        fuse_p = K->sym_state == 1 && opts.fp32_storage == SFEM_FP32_UPPER && chunk % 2 == 0;
+        if (fuse_p) SFEM_TRY(alloc(&p2, nd, "p (second buffer)"));
+    }
     auto enqueue_iter = [&](int slot) {
-        k_update_p<T><<<vec_grid, 256, 0, ctx->stream>>>(nd, v.p, v.z, S);
-        SFEM_LAUNCHED(ctx);
-        if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
-        launch_spmv<T, B>(val, v.p, v.q, true);
-        if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
+        T *pcur = v.p;
+        bool done_spmv = false;
+        if constexpr (sizeof(T) == 4) {
+            if (fuse_p) {
+                T *pin = (slot % 2 == 0) ? v.p : p2, *pout = (slot % 2 == 0) ? p2 : v.p;
+                if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
+                auto kern = k_spmv_sym<float, B, 1, true>;
+                kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN,
+                                                             m->nslices, pin, v.q, fixed, S, partial, v.z, pout);
+                SFEM_LAUNCHED(ctx);
+                if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
+                pcur = pout;
+                done_spmv = true;
+            }
+        }
+        if (!done_spmv) {
+            k_update_p<T><<<vec_grid, 256, 0, ctx->stream>>>(nd, v.p, v.z, S);
+            SFEM_LAUNCHED(ctx);
+            if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
+            launch_spmv<T, B>(val, v.p, v.q, true);
+            if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
+        }
         {
             auto kern = k_update_node<T, B, PC, MIXED>;
             kern<<<resident_grid(ctx, kern, UPD_T, upd_grid), UPD_T, 0, ctx->stream>>>(
-                m->nN, v.x, v.r, v.z, v.p, v.q, v.minv, S, partial);
+                m->nN, v.x, v.r, v.z, pcur, v.q, v.minv, S, partial);
         }
         SFEM_LAUNCHED(ctx);
         if constexpr (MIXED) {
@@ -740,7 +784,7 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
             ctx->launches += 3;
         }
     };
-    const int per_iter = MIXED ? 6 : 3;
+    const int per_iter = (MIXED ? 6 : 3) - (fuse_p ? 1 : 0);
     if (profile) {
         events.resize(2 * chunk);
         for (auto &e : events) SFEM_CUDA(ctx, cudaEventCreate(&e));
