@@ -385,6 +385,10 @@ typedef struct {
     double idle_exit_ms;       /* the kernel leaves after this long without work;
                                   the server relaunches it on the next request   */
     sfem_solve_opts solve;     /* precision, precond, rtol, maxit, reliable_delta */
+    int warm_start;            /* != 0: a request with a topology key starts from
+                                  the last solution served on that key (kept on
+                                  the GPU); results then depend, within the
+                                  tolerance, on what was served before          */
 } sfem_server_config;
 
 typedef struct {

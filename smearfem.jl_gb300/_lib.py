@@ -57,7 +57,8 @@ class BatchStats(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("cluster", C.c_int), ("threads", C.c_int), ("sm_fraction", C.c_double),
                 ("hbm_budget_fraction", C.c_double), ("hbm_budget_bytes", C.c_int64),
-                ("max_inflight", C.c_int), ("idle_exit_ms", C.c_double), ("solve", SolveOpts)]
+                ("max_inflight", C.c_int), ("idle_exit_ms", C.c_double), ("solve", SolveOpts),
+                ("warm_start", C.c_int)]
 
 
 class ServerResult(C.Structure):

@@ -105,6 +105,7 @@ struct BatchArgs {
     int64_t nd;
     double *u_out;
     int64_t u_len;   // entries of u_out (zeroed by the serving kernel)
+    const double *u_init;  // initial guess in u_out's numbering (a previous solution), or null
     // solver
     double rtol, delta2;
     int maxit, block_jacobi;
@@ -806,18 +807,40 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
         G.sync();
 
         // ---- 5. preconditioned CG
-        double rz = 0.0, bb = 0.0;
+        // warm start: x = the free part of u_init (in x64 for the mixed
+        // solver, whose FP32 iterate is a correction; in x for FP64), and the
+        // initial residual b - K x in FP64
+        const bool warm = a.u_init != nullptr;
+        if (warm) {
+            double *x0 = MIXED ? a.x64 : (double *)(void *)xv;
+            for (int64_t node = n0 + gt; node < n1; node += gstride) {
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    const int64_t d = node * B + i;
+                    const int64_t g = internal_to_output<B>(a, M, node, i);
+                    x0[d] = (g >= 0 && !a.fixed[d]) ? a.u_init[g] : 0.0;
+                }
+            }
+            G.sync();
+            grp_spmv<double, B, false, 2>(a.sliceptr, a.col, a.val64, M.slice0 + gw, M.slice1, gnw, n1, x0, nullptr, 0.0,
+                                          nullptr, a.q64, a.fixed, true);
+            G.sync();
+        }
+        double rz = 0.0, bb = 0.0, rr0 = 0.0;
         {
-            double prz = 0.0, pbb = 0.0;
+            double prz = 0.0, pbb = 0.0, prr = 0.0;
             for (int64_t node = n0 + gt; node < n1; node += gstride) {
                 T r[B];
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
-                    const double bv = a.b64[node * B + i];
-                    r[i] = (T)bv;
-                    rv[node * B + i] = r[i];
-                    pv[node * B + i] = T(0);
+                    const int64_t d = node * B + i;
+                    const double bv = a.b64[d];
+                    const double r0 = warm ? (a.fixed[d] ? 0.0 : bv - a.q64[d]) : bv;
+                    r[i] = (T)r0;
+                    rv[d] = r[i];
+                    pv[d] = T(0);
                     pbb += bv * bv;
+                    prr += r0 * r0;
                 }
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
@@ -831,11 +854,12 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
             const double2 t = G.sum2(prz, pbb, red, xch, ph++);
             rz = t.x;
             bb = t.y;
+            rr0 = warm ? G.sum2(prr, 0.0, red, xch, ph++).x : bb;
         }
         const double tol2 = a.rtol * a.rtol * bb;
-        double rr_ref = bb, rr = bb, beta = 0.0;
+        double rr_ref = rr0, rr = rr0, beta = 0.0;
         int it = 0, refreshes = 0, status = G.max_flag(s_flag);
-        bool done = status != SFEM_OK || !(bb > 0.0);
+        bool done = status != SFEM_OK || !(bb > 0.0) || rr0 <= tol2;
         while (!done) {
             // q = K p with p = z + beta p_prev formed inside the SpMV (stored to pw)
             constexpr int US = sizeof(T) == 8 ? 2 : UF, WS = sizeof(T) == 8 ? 0 : WF;

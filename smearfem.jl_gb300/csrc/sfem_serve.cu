@@ -248,6 +248,8 @@ __global__ void __launch_bounds__(512, 1) k_serve(const __grid_constant__ ServeT
 struct Topology {
     sfem_mesh *mesh = nullptr;
     int refs = 0;
+    double *warm = nullptr;  // last solution served on this topology (warm starts)
+    bool warm_valid = false;
 };
 
 struct Request {
@@ -316,7 +318,7 @@ int64_t request_bytes(int ndim, int nen, int b, int64_t nN, int64_t nEl, int64_t
     bytes += 8 * (int64_t)sfem_npairs(nen) * b * b * nEl;         // element stiffness
     bytes += (8 + 4) * nslabs * 32 * b * b;                       // K fp64 + fp32
     bytes += 2 * nd + 8 * 4 * nd + 8 * (6 * nd + nd * b);         // masks, FP64 vectors, CG vectors + minv
-    bytes += 8 * b * nN;                                          // u
+    bytes += 8 * b * nN * 2;                                      // u, initial guess (warm starts)
     return bytes;
 }
 
@@ -478,6 +480,19 @@ int place_request(sfem_server *s, Request *r) {
     SFEM_TRY(alloc((void **)&q64, sizeof(double) * ndp, "request q"));
     SFEM_TRY(alloc(&vecT, sizeof(double) * (6 * ndp + ndp * b), "request CG vectors"));
     SFEM_TRY(alloc((void **)&u, sizeof(double) * (b * nN + 1), "request u"));
+    double *u0 = nullptr;
+    if (s->cfg.warm_start && r->key != 0) {  // a private copy: the topology's buffer moves on
+        const double *w = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            auto it = s->topo.find(r->key);
+            if (it != s->topo.end() && it->second.warm_valid) w = it->second.warm;
+        }
+        if (w) {
+            SFEM_TRY(alloc((void **)&u0, sizeof(double) * (b * nN), "request initial guess"));
+            SFEM_CUDA(ctx, cudaMemcpyAsync(u0, w, sizeof(double) * b * nN, cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+    }
     SFEM_TRY(sfem_copy_in(ctx, X, r->X.data(), sizeof(double) * nd_ * nN, SFEM_MEM_HOST));
     SFEM_TRY(sfem_copy_in(ctx, E, r->E.data(), sizeof(double) * r->E.size(), SFEM_MEM_HOST));
     SFEM_TRY(sfem_copy_in(ctx, NU, r->nu.data(), sizeof(double) * r->nu.size(), SFEM_MEM_HOST));
@@ -535,6 +550,7 @@ int place_request(sfem_server *s, Request *r) {
     a.nd = ndp;
     a.u_out = u;
     a.u_len = b * nN;
+    a.u_init = u0;
     a.rtol = s->cfg.solve.rtol;
     a.delta2 = s->cfg.solve.reliable_delta * s->cfg.solve.reliable_delta;
     a.maxit = s->cfg.solve.maxit > 0 ? s->cfg.solve.maxit : 1000000;
@@ -628,6 +644,15 @@ void worker_loop(sfem_server *s) {
             lk.lock();
             r->stats = s->h_stats[r->slot];
             r->trace = s->h_trace[r->slot];
+            if (s->cfg.warm_start && r->key != 0 && r->stats.status == SFEM_OK) {
+                Topology &t = s->topo[r->key];
+                if (!t.warm && sfem_dalloc(s->ctx, (void **)&t.warm, sizeof(double) * r->ndof, "warm start") != SFEM_OK)
+                    t.warm = nullptr;
+                if (t.warm && cudaMemcpyAsync(t.warm, r->d_u, sizeof(double) * r->ndof, cudaMemcpyDeviceToDevice,
+                                              s->ctx->stream) == cudaSuccess)
+                    t.warm_valid = true;
+                cudaGetLastError();
+            }
             r->status = r->stats.status;
             release_request_buffers(s, r);
             s->bytes_in_use -= r->need;
@@ -869,8 +894,10 @@ extern "C" int sfem_server_destroy(sfem_server *s) {
     if (s->h_stop) *(volatile int *)s->h_stop = 1;
     if (s->compute) cudaStreamSynchronize(s->compute);
     for (auto &kv : s->requests) delete kv.second;
-    for (auto &kv : s->topo)
+    for (auto &kv : s->topo) {
+        if (kv.second.warm) sfem_dfree(s->ctx, kv.second.warm);
         if (kv.second.mesh) sfem_mesh_release(kv.second.mesh);
+    }
     if (s->ring) cudaFree(s->ring);
     if (s->head) cudaFree(s->head);
     if (s->h_tail) cudaFreeHost(s->h_tail);

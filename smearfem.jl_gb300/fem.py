@@ -482,7 +482,8 @@ class Server:
     """
 
     def __init__(self, cluster=4, threads=512, sm_fraction=0.9, hbm_budget_fraction=0.5,
-                 hbm_budget_bytes=0, max_inflight=1024, idle_exit_ms=20.0, device=0, **solve_kw):
+                 hbm_budget_bytes=0, max_inflight=1024, idle_exit_ms=20.0, warm_start=False, device=0,
+                 **solve_kw):
         cfg = L.ServerConfig()
         lib().sfem_server_config_default(C.byref(cfg))
         cfg.cluster, cfg.threads = int(cluster), int(threads)
@@ -491,6 +492,7 @@ class Server:
         cfg.hbm_budget_bytes = int(hbm_budget_bytes)
         cfg.max_inflight = int(max_inflight)
         cfg.idle_exit_ms = float(idle_exit_ms)
+        cfg.warm_start = 1 if warm_start else 0
         kw = {"precision": "mixed", "precond": "block_jacobi", "rtol": 1e-8}
         kw.update(solve_kw)
         cfg.solve = _solve_opts(**kw)

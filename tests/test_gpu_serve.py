@@ -200,6 +200,30 @@ def test_mixed_classes_in_one_stream(sfem, ctx):
 
 
 @pytest.mark.timeout(300)
+def test_warm_start_state_per_topology(sfem, ctx):
+    """With warm starts a request starts from the last solution served on its
+    topology key: a repeated request needs no iteration, a nearby one fewer;
+    every result stays within the tolerance of its own single-mesh solve."""
+    mg = sfem.meshgen
+    p = mg.quad_problem(40, 77, jitter=0.15, nu_range=(0.2, 0.45), e_sigma=0.3, plane="strain")
+    q = mg.quad_problem(40, 77, jitter=0.15, nu_range=(0.2, 0.45), e_sigma=0.3, plane="strain")
+    q.Young = p.Young * 1.02                                   # same mesh and loads, stiffer material
+    q.fixed_vals = p.fixed_vals * 1.05
+    with _server(sfem, warm_start=True) as srv:
+        cold = srv.wait(_submit(srv, p, key=40), timeout_ms=60000)
+        again = srv.wait(_submit(srv, p, key=40, with_ien=False), timeout_ms=60000)
+        near = srv.wait(_submit(srv, q, key=40, with_ien=False), timeout_ms=60000)
+    ref_p, ref_q = _single(sfem, ctx, p), _single(sfem, ctx, q)
+    assert cold[1]["status"] == 0 and again[1]["status"] == 0 and near[1]["status"] == 0
+    assert again[1]["iterations"] == 0 and near[1]["iterations"] < cold[1]["iterations"]
+    assert _rel(cold[0], ref_p) <= TOL_U and _rel(again[0], ref_p) <= TOL_U and _rel(near[0], ref_q) <= TOL_U
+    with _server(sfem) as srv:                                  # off: repeats are bitwise identical
+        a = srv.wait(_submit(srv, p, key=40), timeout_ms=60000)
+        b = srv.wait(_submit(srv, p, key=40, with_ien=False), timeout_ms=60000)
+    assert np.array_equal(a[0], b[0]) and a[1]["iterations"] == b[1]["iterations"] == cold[1]["iterations"]
+
+
+@pytest.mark.timeout(300)
 def test_errors_and_shutdown_with_work_outstanding(sfem, ctx):
     probs = _quads([6, 10], seed=2)
     with _server(sfem) as srv:
