@@ -70,6 +70,9 @@ def parse_args(argv=None):
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
     ap.add_argument("--serve-requests", type=int, default=240, help="requests in the saturating stream")
     ap.add_argument("--serve-pool", type=int, default=96, help="distinct meshes the stream draws from")
+    ap.add_argument("--serve-precond", default="multigrid", choices=["multigrid", "block_jacobi"],
+                    help="serving preconditioner (multigrid: structured meshes, cached per topology)")
+    ap.add_argument("--serve-launch", default="8,256", help="cluster,threads of the serving kernel")
     ap.add_argument("--no-extras", action="store_true", help="same as --legs value")
     a = ap.parse_args(argv)
     a.legs = {"value"} if a.no_extras else set(x.strip() for x in a.legs.split(",") if x.strip())
@@ -398,7 +401,9 @@ def our_arm(args, dist):
         nnzb = nnz // 9
         up_blocks = (nnzb - nN) // 2 + nN
         lo_blocks = (nnzb - nN) // 2
-        sym_bytes = up_blocks * (36 + 4) + lo_blocks * 8 + 3 * nN * (4 + 4 + 1)
+        # per DOF: the old direction and z read, the new direction and y written
+        # (the direction update runs inside this SpMV), the fixed flag
+        sym_bytes = up_blocks * (36 + 4) + lo_blocks * 8 + 3 * nN * (4 * 4 + 1)
         hbm_peak, peak_kind = measured_peaks()
         line["mixed"] = {"value": vmix, "ms_per_step": msm,
                          "precond": "block_jacobi", "iterations": infm[-1]["iterations"],
@@ -634,6 +639,39 @@ def _sustained(recs, ndof_of):
     return len(done) / win, sum(ndof_of(k) for k, _ in done) / win
 
 
+def _cg_iteration_bytes(p):
+    """Algorithmic memory traffic of one FP32 CG iteration of the per-mesh
+    solver on structured mesh p: every stored b x b block of K and its column
+    index once ((3 ne + 1)^ndim blocks), plus per DOF the SpMV's own-row reads
+    of p and z, writes of the new p and of q and the fixed flag (17 B), and the
+    update's reads of x, r, p, q and the nodal inverse and writes of x, r, z
+    (28 + 4 b B)."""
+    b = p.ndim
+    nnzb = (3 * p.ne + 1) ** b
+    return nnzb * (4 * b * b + 4) + p.n_dof * (17 + 28 + 4 * b)
+
+
+def _window_traffic(recs, pool):
+    """Memory traffic rate of the CG iterations over the saturated window
+    (the requests _sustained counts) and the share of group time per class."""
+    claims = [r["t_claim_ms"] for _, _, r in recs]
+    t0, t1 = min(claims), max(claims)
+    done = [(k, r) for k, _, r in recs if t0 < r["t_end_ms"] <= t1]
+    if t1 <= t0 or not done:
+        return None
+    nbytes = sum(r["iterations"] * _cg_iteration_bytes(pool[k]) for k, r in done)
+    gt = {2: 0.0, 3: 0.0}
+    its = {2: [], 3: []}
+    for k, _, r in recs:
+        gt[pool[k].ndim] += r["gpu_ms"]
+        its[pool[k].ndim].append(r["iterations"])
+    tot = sum(gt.values())
+    return {"gbs": nbytes / ((t1 - t0) * 1e-3) / 1e9,
+            "group_time_share": {"quads": gt[2] / tot, "hexes": gt[3] / tot},
+            "iterations_median": {"quads": float(np.median(its[2])) if its[2] else None,
+                                  "hexes": float(np.median(its[3])) if its[3] else None}}
+
+
 def _concurrency(recs):
     """Mean number of requests on the GPU at once over the stream (device clock)."""
     iv = [(r["t_claim_ms"], r["t_end_ms"]) for _, _, r in recs]
@@ -654,7 +692,8 @@ def serve_leg(args, pkg, ctx, dist):
     # the whole GPU for the kernel: after the warm-up every topology is cached, so
     # no pattern build needs free SMs during the measured streams
     # 8-CTA clusters of 256 threads (two per SM): measured 5% above 4 x 512 on this stream
-    srv = pkg.Server(precision="mixed", precond="block_jacobi", rtol=rtol, cluster=8, threads=256,
+    cl, th = (int(v) for v in args.serve_launch.split(","))
+    srv = pkg.Server(precision="mixed", precond=args.serve_precond, rtol=rtol, cluster=cl, threads=th,
                      sm_fraction=1.0, idle_exit_ms=200.0)
     try:
         # warm-up: every pool mesh once (builds and caches each topology's pattern)
@@ -671,6 +710,7 @@ def serve_leg(args, pkg, ctx, dist):
         same = sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs)
         capacity = n / wall
         sus_rps, sus_dps = _sustained(recs, lambda k: pool[k].n_dof)
+        traffic = _window_traffic(recs, pool)
         peak = srv.info()
         # below capacity: latency without a backlog
         m = max(20, min(120, int(capacity * 8)))
@@ -701,7 +741,10 @@ def serve_leg(args, pkg, ctx, dist):
     pct = lambda a, q: float(np.percentile(a, q))  # noqa: E731
     return {"workload": f"open-loop Poisson stream at {args.serve_rate:g} req/s, {n} requests "
                         f"from a pool of {len(pool)} meshes (70% quads n~U{{32..512}}, 30% hexes "
-                        f"n~U{{16..64}}), mixed block-Jacobi PCG to {rtol:g}",
+                        f"n~U{{16..64}}), mixed-precision PCG to {rtol:g}, "
+                        + ("geometric multigrid V(1,1) cached per topology" if args.serve_precond == "multigrid"
+                           else "block Jacobi"),
+            "precond": args.serve_precond, "launch": {"cluster": cl, "threads": th},
             "solves_per_s": capacity, "dof_per_s": dofs / wall, "unit": "requests/s",
             "sustained": {"solves_per_s": sus_rps, "dof_per_s": sus_dps,
                           "window": "first to last claim of the stream (device clock): requests always "
@@ -714,6 +757,12 @@ def serve_leg(args, pkg, ctx, dist):
             "warmup_s": t_warm, "peak_inflight": peak["peak_inflight"], "peak_bytes": info["peak_bytes"],
             "kernel_launches": info["kernel_launches"], "grid_ctas": info["grid"], "cluster": info["cluster"],
             "gpu_concurrency": _concurrency(recs),
+            "cg_memory": None if traffic is None else {
+                "achieved_gbs": traffic["gbs"], "frac_hbm": traffic["gbs"] / measured_peaks()[0],
+                "basis": "iterations x (K blocks + column indices + 11 FP32 vectors per DOF) of the "
+                         "requests finished in the saturated window, over that window",
+                "group_time_share": traffic["group_time_share"],
+                "iterations_median": traffic["iterations_median"]},
             "rel_err_max_sample": max(errs),
             "plain_fp64_gpu": {"dof_per_s": dof_plain / t_plain,
                                "path": "single-mesh API per request: assemble + FP64 Jacobi-PCG, "

@@ -64,7 +64,9 @@ enum { SFEM_MEM_HOST = 0, SFEM_MEM_DEVICE = 1 };
 enum { SFEM_Q1 = 1, SFEM_Q2 = 2 };                      /* FunctionClass              */
 enum { SFEM_PLANE_STRESS = 0, SFEM_PLANE_STRAIN = 1 };  /* 2D elasticity law          */
 enum { SFEM_FP64 = 0, SFEM_MIXED = 1 };                 /* solver precision           */
-enum { SFEM_PC_JACOBI = 0, SFEM_PC_BLOCK_JACOBI = 1 };  /* preconditioner             */
+enum { SFEM_PC_JACOBI = 0, SFEM_PC_BLOCK_JACOBI = 1,  /* preconditioner             */
+       SFEM_PC_MULTIGRID = 2 };  /* batch and server, mixed precision: geometric multigrid on
+                                    structured (meshgrid) Q1 meshes, block Jacobi otherwise */
 enum { SFEM_FP32_UPPER = 0, SFEM_FP32_FULL = 1 };       /* mixed-precision K storage  */
 
 typedef struct sfem_ctx sfem_ctx;
@@ -185,7 +187,8 @@ SFEM_API int sfem_matrix_destroy(sfem_matrix *K);
 
 typedef struct {
     int precision;        /* SFEM_FP64 (default) or SFEM_MIXED                    */
-    int precond;          /* SFEM_PC_JACOBI (default) or SFEM_PC_BLOCK_JACOBI     */
+    int precond;          /* SFEM_PC_JACOBI (default) or SFEM_PC_BLOCK_JACOBI;
+                             SFEM_PC_MULTIGRID in batches and servers          */
     double rtol;          /* stop at ||f_f - K_ff u_f|| <= rtol ||f_f - K_fd u_d|| */
     int maxit;            /* iteration cap (SFEM_NOT_CONVERGED beyond it)          */
     int check_every;      /* iterations per device-side chunk between host checks */

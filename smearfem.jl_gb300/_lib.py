@@ -22,7 +22,7 @@ MEM_HOST, MEM_DEVICE = 0, 1
 Q1, Q2 = 1, 2
 PLANE_STRESS, PLANE_STRAIN = 0, 1
 FP64, MIXED = 0, 1
-PC_JACOBI, PC_BLOCK_JACOBI = 0, 1
+PC_JACOBI, PC_BLOCK_JACOBI, PC_MULTIGRID = 0, 1, 2
 FP32_UPPER, FP32_FULL = 0, 1
 
 

@@ -24,6 +24,8 @@
 
 namespace cgrp = cooperative_groups;
 
+struct MgMesh;  // multigrid hierarchy of one structured mesh (sfem_mg.cuh)
+
 struct BatchMesh {
     int64_t node0, nnode;      // combined (padded) node range start, real node count
     int64_t slice0, slice1;    // its slices
@@ -106,6 +108,7 @@ struct BatchArgs {
     double *u_out;
     int64_t u_len;   // entries of u_out (zeroed by the serving kernel)
     const double *u_init;  // initial guess in u_out's numbering (a previous solution), or null
+    const MgMesh *mg;      // per mesh: multigrid hierarchy (used when its nlev >= 2), or null
     // solver
     double rtol, delta2;
     int maxit, block_jacobi;
@@ -216,12 +219,21 @@ __device__ __forceinline__ T spmv_operand(const T *__restrict__ x, const T *__re
 // streaming hint, which leaves the L1 to the gathered vector entries.  The
 // products are added in slab order on every path, so sums do not depend on
 // U, W or the path taken.
-template <typename T, int B, bool FUSE_P, int U, int W = 0>
+//
+// EPI selects what is stored per row (masked rows always get 0):
+//   SPMV_Y       y = K v, and the v.y share is returned;
+//   SPMV_RES     y = bv - K v (a residual);
+//   SPMV_SMOOTH  y = v + Mv (bv - K v) with Mv the row's b x b block
+//                ([node][i][j]), one damped block-Jacobi sweep; returns
+//                this thread's bv.y share.
+enum { SPMV_Y = 0, SPMV_RES = 1, SPMV_SMOOTH = 2 };
+template <typename T, int B, bool FUSE_P, int U, int W = 0, int EPI = SPMV_Y>
 __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col,
                                            const T *__restrict__ val, int64_t sfirst, int64_t s1, int64_t sstride,
                                            int64_t rend, const T *__restrict__ x, const T *__restrict__ z, T beta,
                                            T *__restrict__ pnew, T *__restrict__ y, const unsigned char *__restrict__ fixed,
-                                           bool masked) {
+                                           bool masked, const T *__restrict__ bv = nullptr,
+                                           const T *__restrict__ Mv = nullptr) {
     constexpr int WP = W > 0 ? W : 1;
     const int lane = threadIdx.x & 31;
     double dot = 0.0;
@@ -310,13 +322,32 @@ __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr,
             }
         }
         if (own) {
+            if constexpr (EPI == SPMV_Y) {
 #pragma unroll
-            for (int i = 0; i < B; ++i) {
-                const int64_t d = r * B + i;
-                if constexpr (FUSE_P) pnew[d] = pd[i];
-                const T out = fx[i] ? T(0) : acc[i];
-                y[d] = out;
-                dot += (double)pd[i] * (double)out;
+                for (int i = 0; i < B; ++i) {
+                    const int64_t d = r * B + i;
+                    if constexpr (FUSE_P) pnew[d] = pd[i];
+                    const T out = fx[i] ? T(0) : acc[i];
+                    y[d] = out;
+                    dot += (double)pd[i] * (double)out;
+                }
+            } else {
+                T res[B];
+#pragma unroll
+                for (int i = 0; i < B; ++i) res[i] = fx[i] ? T(0) : bv[r * B + i] - acc[i];
+                if constexpr (EPI == SPMV_RES) {
+#pragma unroll
+                    for (int i = 0; i < B; ++i) y[r * B + i] = res[i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < B; ++i) {
+                        T o = pd[i];
+#pragma unroll
+                        for (int j = 0; j < B; ++j) o = fma(Mv[(r * B + i) * B + j], res[j], o);
+                        y[r * B + i] = o;
+                        dot += (double)bv[r * B + i] * (double)o;
+                    }
+                }
             }
         }
         if constexpr (W > 0) {
@@ -480,12 +511,18 @@ struct ClusterGroup {
     }
 };
 
+}  // namespace sfem_dev
+
+#include "sfem_mg.cuh"
+
+namespace sfem_dev {
+
 // Assemble and solve mesh `mb` with group G (a CTA or a cluster).
 // UF: slabs in flight per thread in the CG loop's SpMV, WF: slice width of
 // its pipelined path (0: none), NV: nodes per thread and step of the vector
 // update.  The register budget of the calling kernel decides what fits.
 template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF = 4, int WF = 0, int NVF = 1,
-          bool SPMV_CALL = false, bool UPD_CALL = false>
+          bool SPMV_CALL = false, bool UPD_CALL = false, bool MG = false>
 __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
                              int *s_flag) {
     using T = typename std::conditional<MIXED, float, double>::type;
@@ -506,6 +543,22 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
     int ph = 0;           // parity of the reduction buffers
     const T *valT = MIXED ? (const T *)a.val32 : (const T *)a.val64;
     const BatchMesh M = a.meshes[mb];
+    // multigrid (MG): structured Q1 meshes in the mixed solver; compiled only
+    // into the instantiations that ask for it, so the others keep their
+    // register allocation
+    constexpr bool MGOK = MG && MIXED && NEN == (1 << NDIM);
+    const MgMesh *mgp = nullptr;
+    if constexpr (MGOK) {
+        if (a.mg && a.mg[mb].nlev >= 2) mgp = a.mg + mb;
+    }
+    T *zpre = zv;           // where the vector updates put M^-1 r: z, or the
+    const T *mpre = minv;   // multigrid's pre-smoothing sweep
+    if constexpr (MGOK) {
+        if (mgp) {
+            zpre = mgp->lev[0].x;
+            mpre = mgp->lev[0].minv;
+        }
+    }
     unsigned long long t_start = 0;
     if (tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
     {
@@ -805,6 +858,9 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                 for (int j = 0; j < B; ++j) minv[(node * B + i) * B + j] = (T)I[i][j];
         }
         G.sync();
+        if constexpr (MGOK) {
+            if (mgp) mg_setup<Grp, NDIM, B>(G, a, M, mgp, minv, s_flag);
+        }
 
         // ---- 5. preconditioned CG
         // warm start: x = the free part of u_init (in x64 for the mixed
@@ -846,9 +902,16 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                 for (int i = 0; i < B; ++i) {
                     T zi = T(0);
 #pragma unroll
-                    for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
-                    zv[node * B + i] = zi;
+                    for (int j = 0; j < B; ++j) zi = fma(mpre[(node * B + i) * B + j], r[j], zi);
+                    zpre[node * B + i] = zi;
                     prz += (double)(r[i] * zi);
+                }
+            }
+            constexpr int USM = sizeof(T) == 8 ? 2 : UF, WSM = sizeof(T) == 8 ? 0 : WF;
+            if constexpr (MGOK) {
+                if (mgp) {
+                    G.sync();
+                    prz = mg_vcycle<Grp, NDIM, B, USM, WSM>(G, a, M, mgp, rv, zv);
                 }
             }
             const double2 t = G.sum2(prz, pbb, red, xch, ph++);
@@ -885,11 +948,17 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
             {
                 double2 pr;
                 if constexpr (UPD_CALL)
-                    pr = cg_update_call<T, B, NVF>(xv, rv, zv, pv, qv, minv, alpha, n0, n1, gt, gstride);
+                    pr = cg_update_call<T, B, NVF>(xv, rv, zpre, pv, qv, mpre, alpha, n0, n1, gt, gstride);
                 else
-                    pr = cg_update<T, B, NVF>(xv, rv, zv, pv, qv, minv, alpha, n0, n1, gt, gstride);
+                    pr = cg_update<T, B, NVF>(xv, rv, zpre, pv, qv, mpre, alpha, n0, n1, gt, gstride);
                 prz = pr.x;
                 prr = pr.y;
+                if constexpr (MGOK) {
+                    if (mgp) {
+                        G.sync();
+                        prz = mg_vcycle<Grp, NDIM, B, US, WS>(G, a, M, mgp, rv, zv);
+                    }
+                }
             }
             const double2 t = G.sum2(prz, prr, red, xch, ph++);
             ++it;
@@ -935,9 +1004,15 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                     for (int i = 0; i < B; ++i) {
                         T zi = T(0);
 #pragma unroll
-                        for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], r[j], zi);
-                        zv[node * B + i] = zi;
+                        for (int j = 0; j < B; ++j) zi = fma(mpre[(node * B + i) * B + j], r[j], zi);
+                        zpre[node * B + i] = zi;
                         frz += (double)(r[i] * zi);
+                    }
+                }
+                if constexpr (MGOK) {
+                    if (mgp) {
+                        G.sync();
+                        frz = mg_vcycle<Grp, NDIM, B, US, WS>(G, a, M, mgp, rv, zv);
                     }
                 }
                 const double2 f = G.sum2(frz, frr, red, xch, ph++);
@@ -985,6 +1060,15 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
             a.stats[mb] = st;
         }
     }
+}
+
+// process_mesh with the multigrid preconditioner, as a function of its own: a
+// kernel that also runs meshes without it keeps the register allocation of
+// its other paths (the hierarchy's set-up and cycle are calls).
+template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF, int WF, int NVF, bool SPMV_CALL>
+__device__ __noinline__ void process_mesh_mg(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb,
+                                             double *red, double *xch, int *s_flag) {
+    process_mesh<Grp, NDIM, NEN, NGP, B, MIXED, UF, WF, NVF, SPMV_CALL, false, true>(G, tab, a, mb, red, xch, s_flag);
 }
 
 // 2D classes fit two 512-thread CTAs per SM (64 registers); 3D elasticity

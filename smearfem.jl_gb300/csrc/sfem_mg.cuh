@@ -1,0 +1,641 @@
+// Geometric multigrid preconditioner for the per-mesh solver (process_mesh)
+// on structured Q1 meshes: the node numbering and connectivity of the
+// reference's meshgrid (examples/vector3D.jl:66-101), ne elements per
+// direction, x fastest.
+//
+// Hierarchy.  Level l has n_l elements per direction; n_{l+1} = ceil(n_l / 2)
+// until n <= 2.  Coarse node I sits on fine node c(I) = min(2I, n_l) in each
+// direction (an odd n_l leaves one last interval of width 1).  Prolongation
+// is the tensor product of the 1D interpolation: weight 1 on the coinciding
+// node, 1/2 on an odd fine node between two coarse ones, per displacement
+// component.  Fixed DOFs are taken out on both sides: a fine DOF that is
+// fixed gets no correction, and a coarse DOF is fixed when its coinciding
+// fine DOF is, so P' = diag(free_f) P diag(free_c).
+//
+// Coarse operators are Galerkin products A_{l+1} = P'^T A_l P' with A_0 the
+// masked FP32 K.  Their node pattern is again the 3^ndim neighbourhood, so
+// they are stored as stencils: block (I, I + offset s) at
+// A[(s * B*B + e) * nnode + I], zero where the neighbour is off the grid.
+//
+// Cycle: V(1,1) with l1-scaled block Jacobi (x += w_i D_i^-1 r_i with
+// w_i = (4/3) / rho_i, rho_i = max row sum of |D_i^-1 A_i*|; convergent
+// without eigenvalue estimates since rho(W D^-1 A) <= 4/3) and an exact solve
+// (dense inverse, Gauss-Jordan in FP64) on the coarsest level.  The
+// pre-smoothing sweep from zero is x = w D^-1 r; the post-smoothing sweep
+// is the same operator, so the cycle is a symmetric positive definite
+// preconditioner for CG.
+//
+// Everything is group-wide with plain group barriers between the passes and
+// no atomics on values: a mesh's result does not depend on what else runs.
+//
+// Included by sfem_meshsolve.cuh after the group SpMV and the group types.
+#pragma once
+
+constexpr int MG_MAX_LEVELS = 12;
+
+struct MgLevel {
+    int n;              // elements per direction
+    int nnode;          // (n + 1)^ndim
+    float *A;           // levels >= 1: stencil blocks [s][B*B][nnode]
+    float *minv;        // l1-scaled block-Jacobi inverse [nnode][B][B]
+    unsigned char *fr;  // levels >= 1: 1 for a free DOF [nnode * B]
+    float *x, *b, *t;   // iterate, right-hand side (levels >= 1), residual / smoothed iterate
+};
+
+struct MgMesh {
+    int nlev;  // levels, the fine one included (>= 2)
+    int ndc;   // DOFs of the coarsest level
+    MgLevel lev[MG_MAX_LEVELS];
+    float *cinv;  // inverse of the coarsest operator [ndc][ndc]; fixed rows and columns zero
+    double *gj;   // Gauss-Jordan scratch [ndc][2 ndc]
+};
+
+// Levels of a structured mesh with ne elements per direction (0: too small
+// for a hierarchy).
+inline int mg_levels(int ne) {
+    if (ne < 3) return 0;
+    int L = 1;
+    for (int n = ne; n > 2; n = (n + 1) / 2) ++L;
+    return L <= MG_MAX_LEVELS ? L : 0;
+}
+
+// Device layout of one mesh's hierarchy: the MgMesh record itself, then the
+// arrays, each 256-byte aligned.  With base == nullptr only the size is
+// computed.  ndp: the mesh's padded DOF count (fine vectors follow the CG's).
+inline int64_t mg_layout(int ndim, int B, int ne, int64_t ndp, char *base, MgMesh *out) {
+    const int L = mg_levels(ne);
+    if (L == 0) return 0;
+    int64_t off = 0;
+    auto take = [&](int64_t bytes) -> char * {
+        off = (off + 255) / 256 * 256;
+        char *p = base ? base + off : nullptr;
+        off += bytes > 0 ? bytes : 1;
+        return p;
+    };
+    MgMesh m;
+    memset(&m, 0, sizeof(m));
+    m.nlev = L;
+    take(sizeof(MgMesh));
+    const int S = ndim == 2 ? 9 : 27;
+    int n = ne;
+    for (int l = 0; l < L; ++l) {
+        MgLevel &v = m.lev[l];
+        v.n = n;
+        int64_t nn = 1;
+        for (int d = 0; d < ndim; ++d) nn *= (n + 1);
+        v.nnode = (int)nn;
+        const int64_t nd = l == 0 ? ndp : nn * B;
+        v.minv = (float *)take(sizeof(float) * nn * B * B);
+        v.x = (float *)take(sizeof(float) * nd);
+        v.t = (float *)take(sizeof(float) * nd);
+        if (l > 0) {
+            v.A = (float *)take(sizeof(float) * S * B * B * nn);
+            v.fr = (unsigned char *)take(nn * B);
+            v.b = (float *)take(sizeof(float) * nd);
+        }
+        if (l == L - 1) m.ndc = (int)(nn * B);
+        n = (n + 1) / 2;
+    }
+    m.cinv = (float *)take(sizeof(float) * (int64_t)m.ndc * m.ndc);
+    m.gj = (double *)take(sizeof(double) * 2 * (int64_t)m.ndc * m.ndc);
+    if (out) *out = m;
+    return off;
+}
+
+namespace sfem_dev {
+
+template <int NDIM>
+__device__ __forceinline__ void mg_coords(int64_t i, int n, int c[3]) {
+    const int64_t n1 = n + 1;
+    c[0] = (int)(i % n1);
+    c[1] = (int)((i / n1) % n1);
+    c[2] = NDIM == 3 ? (int)(i / (n1 * n1)) : 0;
+}
+
+template <int NDIM>
+__device__ __forceinline__ int64_t mg_index(const int c[3], int n) {
+    const int64_t n1 = n + 1;
+    return NDIM == 3 ? c[0] + n1 * (c[1] + n1 * (int64_t)c[2]) : c[0] + n1 * c[1];
+}
+
+// 1D interpolation weight of coarse node I at fine node i (fine level of n elements).
+__device__ __forceinline__ float mg_w1(int i, int I, int n) {
+    const int c = min(2 * I, n);
+    if (i == c) return 1.0f;
+    if ((i & 1) && i < n && (i == c - 1 || i == c + 1)) return 0.5f;
+    return 0.0f;
+}
+
+// Stencil position of the neighbour offset (j - i), each component in {-1, 0, 1}.
+template <int NDIM>
+__device__ __forceinline__ int mg_stencil(const int ci[3], const int cj[3]) {
+    const int s = (cj[1] - ci[1] + 1) * 3 + (cj[0] - ci[0] + 1);
+    return NDIM == 3 ? (cj[2] - ci[2] + 1) * 9 + s : s;
+}
+
+// Free flags of the DOFs of node ci on level l.
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_free(const BatchArgs &a, const BatchMesh &M, const MgLevel &L, int l,
+                                        const int ci[3], bool f[B]) {
+    const int64_t li = mg_index<NDIM>(ci, L.n);
+#pragma unroll
+    for (int c = 0; c < B; ++c) f[c] = l == 0 ? a.fixed[(M.node0 + li) * B + c] == 0 : L.fr[li * B + c] != 0;
+}
+
+// Block A_l(i, j) of neighbours i, j on level l: the sliced-ELL FP32 K on
+// the fine level (the position of j among i's ascending neighbours follows
+// from the grid), the stencil on coarse levels.  False when the fine
+// pattern is not the structured one.
+template <int NDIM, int B>
+__device__ __forceinline__ bool mg_block(const BatchArgs &a, const BatchMesh &M, const MgLevel &L, int l,
+                                         const int ci[3], const int cj[3], float *blk) {
+    const int64_t li = mg_index<NDIM>(ci, L.n);
+    if (l == 0) {
+        int pos = 0, mul = 1;
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) {
+            const int lo = ci[d] > 0 ? 1 : 0;
+            pos += (cj[d] - ci[d] + lo) * mul;
+            mul *= 1 + lo + (ci[d] < L.n ? 1 : 0);
+        }
+        const int64_t r = M.node0 + li;
+        const int lane = (int)(r & 31);
+        const int64_t slab = a.sliceptr[r >> 5] + pos;
+        if (pos >= a.rowlen[r] || a.col[slab * 32 + lane] != (int)(M.node0 + mg_index<NDIM>(cj, L.n))) return false;
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) blk[e] = a.val32[v32_at<B>(slab, lane, e)];
+    } else {
+        const int s = mg_stencil<NDIM>(ci, cj);
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) blk[e] = L.A[((int64_t)s * B * B + e) * L.nnode + li];
+    }
+    return true;
+}
+
+// Inverse of a B x B block with the rows and columns of fixed DOFs taken
+// out (zero in the result); false if the free part is singular.
+template <int B>
+__device__ __forceinline__ bool mg_inv_block(const double *Din, const bool *f, double *I) {
+    double D[B][B];
+#pragma unroll
+    for (int i = 0; i < B; ++i)
+#pragma unroll
+        for (int j = 0; j < B; ++j) D[i][j] = (f[i] && f[j]) ? Din[i * B + j] : (i == j ? 1.0 : 0.0);
+    double det;
+    double C[B][B];
+    if constexpr (B == 1) {
+        det = D[0][0];
+        C[0][0] = 1.0;
+    } else if constexpr (B == 2) {
+        det = D[0][0] * D[1][1] - D[0][1] * D[1][0];
+        C[0][0] = D[1][1];
+        C[0][1] = -D[0][1];
+        C[1][0] = -D[1][0];
+        C[1][1] = D[0][0];
+    } else {
+        C[0][0] = D[1][1] * D[2][2] - D[1][2] * D[2][1];
+        C[0][1] = D[0][2] * D[2][1] - D[0][1] * D[2][2];
+        C[0][2] = D[0][1] * D[1][2] - D[0][2] * D[1][1];
+        C[1][0] = D[1][2] * D[2][0] - D[1][0] * D[2][2];
+        C[1][1] = D[0][0] * D[2][2] - D[0][2] * D[2][0];
+        C[1][2] = D[0][2] * D[1][0] - D[0][0] * D[1][2];
+        C[2][0] = D[1][0] * D[2][1] - D[1][1] * D[2][0];
+        C[2][1] = D[0][1] * D[2][0] - D[0][0] * D[2][1];
+        C[2][2] = D[0][0] * D[1][1] - D[0][1] * D[1][0];
+        det = D[0][0] * C[0][0] + D[0][1] * C[1][0] + D[0][2] * C[2][0];
+    }
+    if (!(det != 0.0)) return false;
+    const double rd = 1.0 / det;
+#pragma unroll
+    for (int i = 0; i < B; ++i)
+#pragma unroll
+        for (int j = 0; j < B; ++j) I[i * B + j] = (f[i] && f[j]) ? C[i][j] * rd : 0.0;
+    return true;
+}
+
+// Hierarchy set-up after K (FP64 and FP32), the Dirichlet mask and the
+// block-Jacobi inverse `bj` (FP32, [node][B][B]) are in place.  Returns
+// through *flag (group-shared) SFEM_SINGULAR or SFEM_BAD_INDEX on failure.
+template <class Grp, int NDIM, int B>
+__device__ __noinline__ void mg_setup(const Grp &G, const BatchArgs &a, const BatchMesh &M, const MgMesh *mgp,
+                                      const float *bj, int *flag) {
+    constexpr int S = NDIM == 2 ? 9 : 27;
+    const int64_t gt = (int64_t)G.rank() * blockDim.x + threadIdx.x, gstride = (int64_t)G.size() * blockDim.x;
+    const int L = mgp->nlev;
+    // ---- fine level: l1-scaled inverse from the block-Jacobi inverse and the FP32 rows
+    {
+        const MgLevel F = mgp->lev[0];
+        for (int64_t li = gt; li < F.nnode; li += gstride) {
+            const int64_t r = M.node0 + li;
+            float Di[B * B];
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) Di[e] = bj[r * B * B + e];
+            float rs[B];
+#pragma unroll
+            for (int i = 0; i < B; ++i) rs[i] = 0.0f;
+            const int len = a.rowlen[r];
+            const int64_t slab0 = a.sliceptr[r >> 5];
+            const int lane = (int)(r & 31);
+            for (int k = 0; k < len; ++k) {
+                const int64_t slab = slab0 + k;
+                const int c = a.col[slab * 32 + lane];
+                float blk[B * B];
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) blk[e] = a.val32[v32_at<B>(slab, lane, e)];
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) {
+                        if (a.fixed[(int64_t)c * B + j]) continue;
+                        float s = 0.0f;
+#pragma unroll
+                        for (int m = 0; m < B; ++m) s = fmaf(Di[i * B + m], blk[m * B + j], s);
+                        rs[i] += fabsf(s);
+                    }
+            }
+            float rho = 0.0f;
+#pragma unroll
+            for (int i = 0; i < B; ++i) rho = fmaxf(rho, rs[i]);
+            const float w = rho > 0.0f ? (4.0f / 3.0f) / rho : 0.0f;
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) F.minv[r * B * B + e] = w * Di[e];
+        }
+    }
+    // ---- coarse levels
+    for (int l = 0; l + 1 < L; ++l) {
+        const MgLevel F = mgp->lev[l], C = mgp->lev[l + 1];
+        for (int64_t I = gt; I < C.nnode; I += gstride) {  // coarse free flags: the coinciding fine DOF's
+            int cI[3], cf[3] = {0, 0, 0};
+            mg_coords<NDIM>(I, C.n, cI);
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) cf[d] = min(2 * cI[d], F.n);
+            bool f[B];
+            mg_free<NDIM, B>(a, M, F, l, cf, f);
+#pragma unroll
+            for (int c = 0; c < B; ++c) C.fr[I * B + c] = f[c] ? 1 : 0;
+        }
+        G.sync();
+        const int64_t total = (int64_t)C.nnode * S;
+        for (int64_t q = gt; q < total; q += gstride) {
+            const int64_t I = q % C.nnode;
+            const int s = (int)(q / C.nnode);
+            int cI[3], cJ[3] = {0, 0, 0};
+            mg_coords<NDIM>(I, C.n, cI);
+            const int off[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+            bool valid = true;
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) {
+                cJ[d] = cI[d] + off[d];
+                valid = valid && cJ[d] >= 0 && cJ[d] <= C.n;
+            }
+            float acc[B * B];
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) acc[e] = 0.0f;
+            if (valid) {
+                // per direction: fine pairs (i, j), i in supp(I), j in supp(J), |i - j| <= 1
+                int pi[3][7], pj[3][7], np[3] = {1, 1, 1};
+                float pw[3][7];
+                pi[2][0] = pj[2][0] = 0;
+                pw[2][0] = 1.0f;
+#pragma unroll
+                for (int d = 0; d < NDIM; ++d) {
+                    int k = 0;
+                    const int ccI = min(2 * cI[d], F.n);
+                    for (int i = ccI - 1; i <= ccI + 1; ++i) {
+                        if (i < 0 || i > F.n) continue;
+                        const float wi = mg_w1(i, cI[d], F.n);
+                        if (wi == 0.0f) continue;
+                        for (int j = i - 1; j <= i + 1; ++j) {
+                            if (j < 0 || j > F.n) continue;
+                            const float wj = mg_w1(j, cJ[d], F.n);
+                            if (wj == 0.0f) continue;
+                            pi[d][k] = i;
+                            pj[d][k] = j;
+                            pw[d][k] = wi * wj;
+                            ++k;
+                        }
+                    }
+                    np[d] = k;
+                }
+                for (int kz = 0; kz < np[2]; ++kz)
+                    for (int ky = 0; ky < np[1]; ++ky)
+                        for (int kx = 0; kx < np[0]; ++kx) {
+                            const int ci[3] = {pi[0][kx], pi[1][ky], pi[2][kz]};
+                            const int cj[3] = {pj[0][kx], pj[1][ky], pj[2][kz]};
+                            const float w = pw[0][kx] * pw[1][ky] * pw[2][kz];
+                            float blk[B * B];
+                            if (!mg_block<NDIM, B>(a, M, F, l, ci, cj, blk)) {
+                                atomicMax(flag, (int)SFEM_BAD_INDEX);
+                                continue;
+                            }
+                            bool fi[B], fj[B];
+                            mg_free<NDIM, B>(a, M, F, l, ci, fi);
+                            mg_free<NDIM, B>(a, M, F, l, cj, fj);
+#pragma unroll
+                            for (int i = 0; i < B; ++i)
+#pragma unroll
+                                for (int j = 0; j < B; ++j)
+                                    if (fi[i] && fj[j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
+                        }
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j)
+                        if (!C.fr[I * B + i] || !C.fr[mg_index<NDIM>(cJ, C.n) * B + j]) acc[i * B + j] = 0.0f;
+            }
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) C.A[((int64_t)s * B * B + e) * C.nnode + I] = acc[e];
+        }
+        G.sync();
+        if (l + 2 < L) {  // smoother of the new level (the coarsest one is solved exactly)
+            for (int64_t I = gt; I < C.nnode; I += gstride) {
+                double D[B * B], Di[B * B];
+                bool f[B];
+#pragma unroll
+                for (int c = 0; c < B; ++c) f[c] = C.fr[I * B + c] != 0;
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) D[e] = C.A[((int64_t)(S / 2) * B * B + e) * C.nnode + I];
+                if (!mg_inv_block<B>(D, f, Di)) {
+                    atomicMax(flag, (int)SFEM_SINGULAR);
+#pragma unroll
+                    for (int e = 0; e < B * B; ++e) Di[e] = 0.0;
+                }
+                float rs[B];
+#pragma unroll
+                for (int i = 0; i < B; ++i) rs[i] = 0.0f;
+                for (int s = 0; s < S; ++s) {
+                    float blk[B * B];
+#pragma unroll
+                    for (int e = 0; e < B * B; ++e) blk[e] = C.A[((int64_t)s * B * B + e) * C.nnode + I];
+#pragma unroll
+                    for (int i = 0; i < B; ++i)
+#pragma unroll
+                        for (int j = 0; j < B; ++j) {
+                            float v = 0.0f;
+#pragma unroll
+                            for (int m = 0; m < B; ++m) v = fmaf((float)Di[i * B + m], blk[m * B + j], v);
+                            rs[i] += fabsf(v);
+                        }
+                }
+                float rho = 0.0f;
+#pragma unroll
+                for (int i = 0; i < B; ++i) rho = fmaxf(rho, rs[i]);
+                const float w = rho > 0.0f ? (4.0f / 3.0f) / rho : 0.0f;
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) C.minv[I * B * B + e] = w * (float)Di[e];
+            }
+        }
+    }
+    // ---- coarsest level: dense inverse by Gauss-Jordan (one CTA; SPD, no pivoting)
+    if (G.rank() == 0) {
+        const MgLevel C = mgp->lev[L - 1];
+        const int n = mgp->ndc, w2 = 2 * n;
+        double *g = mgp->gj;
+        for (int q = threadIdx.x; q < n * w2; q += blockDim.x) {
+            const int r = q / w2, c = q % w2;
+            double v = 0.0;
+            if (c >= n) {
+                v = (c - n == r) ? 1.0 : 0.0;
+            } else {
+                const int I = r / B, i = r % B, J = c / B, j = c % B;
+                if (!C.fr[I * B + i] || !C.fr[J * B + j]) {
+                    v = (r == c) ? 1.0 : 0.0;
+                } else {
+                    int cI[3], cJ[3];
+                    mg_coords<NDIM>(I, C.n, cI);
+                    mg_coords<NDIM>(J, C.n, cJ);
+                    bool nb = true;
+#pragma unroll
+                    for (int d = 0; d < NDIM; ++d) nb = nb && abs(cI[d] - cJ[d]) <= 1;
+                    if (nb) v = C.A[((int64_t)mg_stencil<NDIM>(cI, cJ) * B * B + i * B + j) * C.nnode + I];
+                }
+            }
+            g[q] = v;
+        }
+        __syncthreads();
+        for (int k = 0; k < n; ++k) {
+            const double piv = g[k * w2 + k];
+            __syncthreads();  // every thread has the pivot before row k changes
+            if (!(piv > 0.0)) {
+                if (threadIdx.x == 0) atomicMax(flag, (int)SFEM_SINGULAR);
+                break;
+            }
+            for (int c = threadIdx.x; c < w2; c += blockDim.x) g[k * w2 + c] /= piv;
+            __syncthreads();
+            for (int q = threadIdx.x; q < n * w2; q += blockDim.x) {
+                const int r = q / w2, c = q % w2;
+                if (r == k || c == k) continue;  // column k is not read again
+                g[q] -= g[r * w2 + k] * g[k * w2 + c];
+            }
+            __syncthreads();
+        }
+        for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+            const int r = q / n, c = q % n;
+            const bool fr = C.fr[(r / B) * B + r % B] && C.fr[(c / B) * B + c % B];
+            mgp->cinv[q] = fr ? (float)g[r * w2 + n + c] : 0.0f;
+        }
+    }
+    G.sync();
+}
+
+// Restriction of level l's residual t_l into b_{l+1}; with `smooth`, also
+// the pre-smoothing sweep from zero x_{l+1} = W D^-1 b_{l+1}.
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_restrict(const BatchMesh &M, const MgLevel &F, const MgLevel &C, int l, bool smooth,
+                                            int64_t gt, int64_t gstride) {
+    for (int64_t I = gt; I < C.nnode; I += gstride) {
+        int cI[3];
+        mg_coords<NDIM>(I, C.n, cI);
+        int fi[3][3], nf[3] = {1, 1, 1};
+        float fw[3][3];
+        fi[2][0] = 0;
+        fw[2][0] = 1.0f;
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) {
+            int k = 0;
+            const int cc = min(2 * cI[d], F.n);
+            for (int i = cc - 1; i <= cc + 1; ++i) {
+                if (i < 0 || i > F.n) continue;
+                const float w = mg_w1(i, cI[d], F.n);
+                if (w == 0.0f) continue;
+                fi[d][k] = i;
+                fw[d][k] = w;
+                ++k;
+            }
+            nf[d] = k;
+        }
+        float acc[B];
+#pragma unroll
+        for (int c = 0; c < B; ++c) acc[c] = 0.0f;
+        for (int kz = 0; kz < nf[2]; ++kz)
+            for (int ky = 0; ky < nf[1]; ++ky)
+                for (int kx = 0; kx < nf[0]; ++kx) {
+                    const int ci[3] = {fi[0][kx], fi[1][ky], fi[2][kz]};
+                    const float w = fw[0][kx] * fw[1][ky] * fw[2][kz];
+                    const int64_t li = mg_index<NDIM>(ci, F.n) + (l == 0 ? M.node0 : 0);
+#pragma unroll
+                    for (int c = 0; c < B; ++c) acc[c] = fmaf(w, F.t[li * B + c], acc[c]);  // t = 0 on fixed DOFs
+                }
+#pragma unroll
+        for (int c = 0; c < B; ++c) {
+            acc[c] = C.fr[I * B + c] ? acc[c] : 0.0f;
+            C.b[I * B + c] = acc[c];
+        }
+        if (smooth) {
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                float v = 0.0f;
+#pragma unroll
+                for (int j = 0; j < B; ++j) v = fmaf(C.minv[(I * B + i) * B + j], acc[j], v);
+                C.x[I * B + i] = v;
+            }
+        }
+    }
+}
+
+// x_l += P' xc (xc: level l+1's iterate, zero on its fixed DOFs).
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_prolong(const BatchArgs &a, const BatchMesh &M, const MgLevel &F, const MgLevel &C,
+                                           int l, const float *xc, int64_t gt, int64_t gstride) {
+    for (int64_t li = gt; li < F.nnode; li += gstride) {
+        int ci[3];
+        mg_coords<NDIM>(li, F.n, ci);
+        int cc[3][2], nc[3] = {1, 1, 1};
+        float cw[3][2];
+        cc[2][0] = 0;
+        cw[2][0] = 1.0f;
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) {
+            const int i = ci[d];
+            if (i == F.n) {
+                cc[d][0] = C.n;
+                cw[d][0] = 1.0f;
+                nc[d] = 1;
+            } else if (!(i & 1)) {
+                cc[d][0] = i / 2;
+                cw[d][0] = 1.0f;
+                nc[d] = 1;
+            } else {
+                cc[d][0] = (i - 1) / 2;
+                cc[d][1] = (i + 1) / 2;
+                cw[d][0] = cw[d][1] = 0.5f;
+                nc[d] = 2;
+            }
+        }
+        float acc[B];
+#pragma unroll
+        for (int c = 0; c < B; ++c) acc[c] = 0.0f;
+        for (int kz = 0; kz < nc[2]; ++kz)
+            for (int ky = 0; ky < nc[1]; ++ky)
+                for (int kx = 0; kx < nc[0]; ++kx) {
+                    const int cI[3] = {cc[0][kx], cc[1][ky], cc[2][kz]};
+                    const float w = cw[0][kx] * cw[1][ky] * cw[2][kz];
+                    const int64_t I = mg_index<NDIM>(cI, C.n);
+#pragma unroll
+                    for (int c = 0; c < B; ++c) acc[c] = fmaf(w, xc[I * B + c], acc[c]);
+                }
+        bool f[B];
+        mg_free<NDIM, B>(a, M, F, l, ci, f);
+        const int64_t d0 = (l == 0 ? M.node0 + li : li) * B;
+#pragma unroll
+        for (int c = 0; c < B; ++c)
+            if (f[c]) F.x[d0 + c] += acc[c];
+    }
+}
+
+// One pass of the coarse-level stencil operator: RES t = b - A x, or SMOOTH
+// out = x + W D^-1 (b - A x).
+template <int NDIM, int B, int EPI>
+__device__ __forceinline__ void mg_stencil_pass(const MgLevel &C, float *out, int64_t gt, int64_t gstride) {
+    constexpr int S = NDIM == 2 ? 9 : 27;
+    for (int64_t I = gt; I < C.nnode; I += gstride) {
+        int cI[3];
+        mg_coords<NDIM>(I, C.n, cI);
+        float acc[B];
+#pragma unroll
+        for (int c = 0; c < B; ++c) acc[c] = 0.0f;
+#pragma unroll 3
+        for (int s = 0; s < S; ++s) {
+            const int cJ[3] = {cI[0] + s % 3 - 1, cI[1] + (s / 3) % 3 - 1, NDIM == 3 ? cI[2] + s / 9 - 1 : 0};
+            bool valid = true;
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) valid = valid && cJ[d] >= 0 && cJ[d] <= C.n;
+            if (!valid) continue;
+            const int64_t J = mg_index<NDIM>(cJ, C.n);
+            float xj[B];
+#pragma unroll
+            for (int c = 0; c < B; ++c) xj[c] = C.x[J * B + c];
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) acc[i] = fmaf(C.A[((int64_t)s * B * B + i * B + j) * C.nnode + I], xj[j], acc[i]);
+        }
+        float res[B];
+#pragma unroll
+        for (int c = 0; c < B; ++c) res[c] = C.fr[I * B + c] ? C.b[I * B + c] - acc[c] : 0.0f;
+        if constexpr (EPI == SPMV_RES) {
+#pragma unroll
+            for (int c = 0; c < B; ++c) out[I * B + c] = res[c];
+        } else {
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                float v = C.x[I * B + i];
+#pragma unroll
+                for (int j = 0; j < B; ++j) v = fmaf(C.minv[(I * B + i) * B + j], res[j], v);
+                out[I * B + i] = v;
+            }
+        }
+    }
+}
+
+// z = V(r): one V(1,1) cycle on the residual r (FP32, the CG's).  On entry
+// the fine level's x holds the pre-smoothing sweep W D^-1 r (written by the
+// caller's vector update).  Returns this thread's r.z share.
+template <class Grp, int NDIM, int B, int U, int W>
+__device__ __noinline__ double mg_vcycle(const Grp &G, const BatchArgs &a, const BatchMesh &M, const MgMesh *mgp,
+                                         const float *r, float *z) {
+    const int tid = threadIdx.x, nw = blockDim.x >> 5;
+    const int64_t gt = (int64_t)G.rank() * blockDim.x + tid, gstride = (int64_t)G.size() * blockDim.x;
+    const int64_t gw = (int64_t)G.rank() * nw + (tid >> 5), gnw = (int64_t)G.size() * nw;
+    const int64_t n1 = M.node0 + M.nnode;
+    const int L = mgp->nlev;
+    const MgLevel F0 = mgp->lev[0];
+    // fine residual t0 = r - A x0
+    grp_spmv<float, B, false, U, W, SPMV_RES>(a.sliceptr, a.col, a.val32, M.slice0 + gw, M.slice1, gnw, n1, F0.x,
+                                              nullptr, 0.0f, nullptr, F0.t, a.fixed, true, r, nullptr);
+    G.sync();
+    for (int l = 1; l < L; ++l) {
+        const MgLevel F = mgp->lev[l - 1], C = mgp->lev[l];
+        mg_restrict<NDIM, B>(M, F, C, l - 1, l + 1 < L, gt, gstride);
+        G.sync();
+        if (l + 1 < L) {
+            mg_stencil_pass<NDIM, B, SPMV_RES>(C, C.t, gt, gstride);
+            G.sync();
+        }
+    }
+    {  // coarsest: x = C^-1 b
+        const MgLevel C = mgp->lev[L - 1];
+        const int n = mgp->ndc;
+        for (int64_t q = gt; q < n; q += gstride) {
+            float v = 0.0f;
+            for (int c = 0; c < n; ++c) v = fmaf(mgp->cinv[q * n + c], C.b[c], v);
+            C.x[q] = v;
+        }
+        G.sync();
+    }
+    const float *xin = mgp->lev[L - 1].x;
+    for (int l = L - 2; l >= 1; --l) {
+        const MgLevel F = mgp->lev[l], C = mgp->lev[l + 1];
+        mg_prolong<NDIM, B>(a, M, F, C, l, xin, gt, gstride);
+        G.sync();
+        mg_stencil_pass<NDIM, B, SPMV_SMOOTH>(F, F.t, gt, gstride);
+        G.sync();
+        xin = F.t;
+    }
+    mg_prolong<NDIM, B>(a, M, F0, mgp->lev[1], 0, xin, gt, gstride);
+    G.sync();
+    return grp_spmv<float, B, false, U, W, SPMV_SMOOTH>(a.sliceptr, a.col, a.val32, M.slice0 + gw, M.slice1, gnw, n1,
+                                                        F0.x, nullptr, 0.0f, nullptr, z, a.fixed, true, r, F0.minv);
+}
+
+}  // namespace sfem_dev

@@ -26,6 +26,7 @@
 // recycled buffer's old contents.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <initializer_list>
 #include <chrono>
 #include <condition_variable>
@@ -208,19 +209,25 @@ __global__ void __launch_bounds__(512, 1) k_serve(const __grid_constant__ ServeT
         // function so that its allocation is not shared with the other classes:
         // measured 17% faster per iteration); the scalar ones stay narrow, which
         // keeps the shared kernel's register allocation nearly free of spills.
+        // Requests with a multigrid hierarchy run the pipeline as a call of its own.
         const ClusterGroup G;
+        const bool mg = MIXED && s_args.mg != nullptr;
         switch (__ldcg(&d->cls)) {
             case CLS_Q1_2D_SCALAR:
-                process_mesh<ClusterGroup, 2, 4, 4, 1, MIXED, 4, 0, 1>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
+                if (mg) process_mesh_mg<ClusterGroup, 2, 4, 4, 1, true, 4, 0, 1, false>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
+                else process_mesh<ClusterGroup, 2, 4, 4, 1, MIXED, 4, 0, 1>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
                 break;
             case CLS_Q1_2D_ELASTIC:
-                process_mesh<ClusterGroup, 2, 4, 4, 2, MIXED, 9, 9, 1>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
+                if (mg) process_mesh_mg<ClusterGroup, 2, 4, 4, 2, true, 9, 9, 1, false>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
+                else process_mesh<ClusterGroup, 2, 4, 4, 2, MIXED, 9, 9, 1>(G, tabs.t[0], s_args, 0, red, xch, &s_flag);
                 break;
             case CLS_Q1_3D_SCALAR:
-                process_mesh<ClusterGroup, 3, 8, 8, 1, MIXED, 4, 0, 1>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
+                if (mg) process_mesh_mg<ClusterGroup, 3, 8, 8, 1, true, 4, 0, 1, false>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
+                else process_mesh<ClusterGroup, 3, 8, 8, 1, MIXED, 4, 0, 1>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
                 break;
             case CLS_Q1_3D_ELASTIC:
-                process_mesh<ClusterGroup, 3, 8, 8, 3, MIXED, 9, 0, 1, true>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
+                if (mg) process_mesh_mg<ClusterGroup, 3, 8, 8, 3, true, 9, 0, 1, true>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
+                else process_mesh<ClusterGroup, 3, 8, 8, 3, MIXED, 9, 0, 1, true>(G, tabs.t[1], s_args, 0, red, xch, &s_flag);
                 break;
             default:
                 process_mesh<ClusterGroup, 2, 9, 4, 1, MIXED, 4, 0, 1>(G, tabs.t[2], s_args, 0, red, xch, &s_flag);
@@ -248,6 +255,7 @@ __global__ void __launch_bounds__(512, 1) k_serve(const __grid_constant__ ServeT
 struct Topology {
     sfem_mesh *mesh = nullptr;
     int refs = 0;
+    int mg_ne = 0;           // elements per direction of a structured (meshgrid) mesh, else 0
     double *warm = nullptr;  // last solution served on this topology (warm starts)
     bool warm_valid = false;
 };
@@ -258,6 +266,7 @@ struct Request {
     std::vector<int64_t> IEN, ID, fdofs;
     int64_t nN = 0, nEl = 0;
     int ndim = 0, fclass = 0, b = 0, nen = 0, plane = 0, cls = 0;
+    int mg_ne = 0;     // multigrid hierarchy of this many elements per direction (0: none)
     int64_t need = 0;  // device bytes while in flight
     // in flight
     int slot = -1;
@@ -320,6 +329,48 @@ int64_t request_bytes(int ndim, int nen, int b, int64_t nN, int64_t nEl, int64_t
     bytes += 2 * nd + 8 * 4 * nd + 8 * (6 * nd + nd * b);         // masks, FP64 vectors, CG vectors + minv
     bytes += 8 * b * nN * 2;                                      // u, initial guess (warm starts)
     return bytes;
+}
+
+int64_t ipow(int64_t b, int e) {
+    int64_t r = 1;
+    for (int i = 0; i < e; ++i) r *= b;
+    return r;
+}
+
+// Elements per direction when the mesh is the reference's structured grid
+// (the node numbering and Q1 connectivity of examples/vector3D.jl:66-101:
+// nodes x fastest, IEN column-major and 1-based), else 0.
+int structured_ne(int ndim, int fclass, int nen, int64_t nN, int64_t nEl, const int64_t *IEN) {
+    if (fclass != SFEM_Q1 || nen != (1 << ndim) || nEl < 1) return 0;
+    int64_t ne = 0;
+    for (int64_t c = std::max<int64_t>(1, (int64_t)std::llround(std::pow((double)nEl, 1.0 / ndim)) - 1);
+         ipow(c, ndim) <= nEl; ++c)
+        if (ipow(c, ndim) == nEl) ne = c;
+    if (ne < 1 || ne > (1 << 20) || ipow(ne + 1, ndim) != nN) return 0;
+    const int64_t n1 = ne + 1, p = n1 * n1;
+    for (int64_t e = 0; e < nEl; ++e) {
+        const int64_t i = e % ne, j = (e / ne) % ne, k = e / (ne * ne);
+        int64_t c[8];
+        if (ndim == 2) {
+            c[0] = j * n1 + i + 1;
+            c[1] = c[0] + 1;
+            c[2] = (j + 1) * n1 + i + 2;
+            c[3] = (j + 1) * n1 + i + 1;
+        } else {
+            const int64_t base = k * p + j * n1 + i + 1;
+            c[0] = base;
+            c[1] = base + 1;
+            c[2] = base + n1 + 1;
+            c[3] = base + n1;
+            c[4] = base + p;
+            c[5] = base + p + 1;
+            c[6] = base + p + n1 + 1;
+            c[7] = base + p + n1;
+        }
+        for (int a = 0; a < nen; ++a)
+            if (IEN[e + a * nEl] != c[a]) return 0;
+    }
+    return (int)ne;
 }
 
 // Dynamic shared memory of process_mesh for one class at `threads` per CTA.
@@ -480,6 +531,14 @@ int place_request(sfem_server *s, Request *r) {
     SFEM_TRY(alloc((void **)&q64, sizeof(double) * ndp, "request q"));
     SFEM_TRY(alloc(&vecT, sizeof(double) * (6 * ndp + ndp * b), "request CG vectors"));
     SFEM_TRY(alloc((void **)&u, sizeof(double) * (b * nN + 1), "request u"));
+    MgMesh *mg = nullptr;
+    if (r->mg_ne > 0) {  // multigrid hierarchy: the record, then its arrays
+        const int64_t mgb = mg_layout(nd_, b, r->mg_ne, ndp, nullptr, nullptr);
+        SFEM_TRY(alloc((void **)&mg, (size_t)mgb, "request multigrid"));
+        MgMesh rec;
+        mg_layout(nd_, b, r->mg_ne, ndp, (char *)mg, &rec);
+        SFEM_CUDA(ctx, cudaMemcpyAsync(mg, &rec, sizeof(rec), cudaMemcpyHostToDevice, ctx->stream));
+    }
     double *u0 = nullptr;
     if (s->cfg.warm_start && r->key != 0) {  // a private copy: the topology's buffer moves on
         const double *w = nullptr;
@@ -554,7 +613,8 @@ int place_request(sfem_server *s, Request *r) {
     a.rtol = s->cfg.solve.rtol;
     a.delta2 = s->cfg.solve.reliable_delta * s->cfg.solve.reliable_delta;
     a.maxit = s->cfg.solve.maxit > 0 ? s->cfg.solve.maxit : 1000000;
-    a.block_jacobi = s->cfg.solve.precond == SFEM_PC_BLOCK_JACOBI ? 1 : 0;
+    a.block_jacobi = s->cfg.solve.precond != SFEM_PC_JACOBI ? 1 : 0;
+    a.mg = mg;
     a.stats = s->d_stats + slot;  // mapped host memory
     a.err = ctx->d_err;
     d.seq = r->seq;
@@ -707,7 +767,8 @@ extern "C" int sfem_server_create(int device, const sfem_server_config *cfg, sfe
     sfem_server_config_default(&c);
     if (cfg) c = *cfg;
     if ((c.cluster != 1 && c.cluster != 2 && c.cluster != 4 && c.cluster != 8) ||
-        (c.threads != 256 && c.threads != 512) || c.max_inflight < 1 || !(c.idle_exit_ms > 0.0))
+        (c.threads != 256 && c.threads != 512) || c.max_inflight < 1 || !(c.idle_exit_ms > 0.0) ||
+        c.solve.precond < SFEM_PC_JACOBI || c.solve.precond > SFEM_PC_MULTIGRID)
         return SFEM_BAD_ARG;
     sfem_server *s = new sfem_server();
     s->cfg = c;
@@ -789,7 +850,9 @@ extern "C" int sfem_server_submit(sfem_server *s, int ndim, int function_class, 
         std::lock_guard<std::mutex> lk(s->mu);
         // a key seen before: its first request carries the connectivity
         cached = topology_key != 0 && s->topo.count(topology_key) != 0;
+        if (cached) r->mg_ne = s->topo[topology_key].mg_ne;
     }
+    const bool want_mg = s->cfg.solve.precond == SFEM_PC_MULTIGRID && s->cfg.solve.precision == SFEM_MIXED;
     if (!cached) {
         if (!IEN || (b > 1 && !ID)) {
             delete r;
@@ -797,6 +860,10 @@ extern "C" int sfem_server_submit(sfem_server *s, int ndim, int function_class, 
         }
         r->IEN.assign(IEN, IEN + nEl * nen);
         if (b > 1) r->ID.assign(ID, ID + nNodes * b);
+        if (want_mg) {
+            const int ne = structured_ne(ndim, function_class, nen, nNodes, nEl, IEN);
+            r->mg_ne = mg_levels(ne) >= 2 ? ne : 0;
+        }
     }
     if (b > 1) {
         r->E.assign(Young, Young + nYoung);
@@ -810,9 +877,10 @@ extern "C" int sfem_server_submit(sfem_server *s, int ndim, int function_class, 
     // footprint estimate from the structured-neighbour bound (27 / 25 / 9 node blocks per row)
     const int64_t width = ndim == 3 ? 27 : (nen == 9 ? 25 : 9);
     r->need = request_bytes(ndim, nen, b, nNodes, nEl, nfix, ((nNodes + 31) / 32) * width);
+    if (r->mg_ne > 0) r->need += mg_layout(ndim, b, r->mg_ne, ((nNodes + 31) / 32) * 32 * b, nullptr, nullptr);
     r->t_submit = std::chrono::steady_clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
-    if (topology_key != 0 && !cached) s->topo[topology_key];  // placed (pattern built) in submission order
+    if (topology_key != 0 && !cached) s->topo[topology_key].mg_ne = r->mg_ne;  // placed in submission order
     r->id = s->next_id++;
     s->requests[r->id] = r;
     s->pending.push_back(r);

@@ -281,7 +281,7 @@ class Matrix:
         opts = L.SolveOpts()
         lib().sfem_solve_opts_default(C.byref(opts))
         opts.precision = {"fp64": L.FP64, "mixed": L.MIXED}[precision]
-        opts.precond = {"jacobi": L.PC_JACOBI, "block_jacobi": L.PC_BLOCK_JACOBI}[precond]
+        opts.precond = _PRECOND[precond]
         opts.rtol = rtol
         opts.maxit = maxit
         opts.check_every = check_every
@@ -356,12 +356,17 @@ class Matrix:
             pass
 
 
+# "multigrid": batches and servers, mixed precision; geometric multigrid on
+# structured (meshgrid) Q1 meshes, block Jacobi on the others
+_PRECOND = {"jacobi": L.PC_JACOBI, "block_jacobi": L.PC_BLOCK_JACOBI, "multigrid": L.PC_MULTIGRID}
+
+
 def _solve_opts(precision="fp64", precond="jacobi", rtol=1e-10, maxit=100000, check_every=32,
                 reliable_delta=0.1, profile=False, fp32_storage="upper"):
     opts = L.SolveOpts()
     lib().sfem_solve_opts_default(C.byref(opts))
     opts.precision = {"fp64": L.FP64, "mixed": L.MIXED}[precision]
-    opts.precond = {"jacobi": L.PC_JACOBI, "block_jacobi": L.PC_BLOCK_JACOBI}[precond]
+    opts.precond = _PRECOND[precond]
     opts.rtol = rtol
     opts.maxit = maxit
     opts.check_every = check_every
