@@ -67,6 +67,8 @@ def parse_args(argv=None):
                     help="threads,ctas_per_sm,cluster,cluster_min_nodes: fixed batch launch shape (no autotune)")
     ap.add_argument("--batch-rtol", type=float, default=1e-12,
                     help="batch-leg relative residual (1e-12 keeps the error in u under 1e-8)")
+    ap.add_argument("--batch-precond", default="multigrid", choices=["multigrid", "block_jacobi"],
+                    help="batch-leg preconditioner (multigrid: structured meshes)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
     ap.add_argument("--serve-requests", type=int, default=240, help="requests in the saturating stream")
     ap.add_argument("--serve-pool", type=int, default=96, help="distinct meshes the stream draws from")
@@ -536,12 +538,12 @@ def batch_leg(args, pkg, ctx, stream, dist):
         shape, tuned_ms = bt.launch(), None
     else:
         shape, tuned_ms = bt.autotune(1.0, nus, fixed, vals, plane="strain", precision="mixed",
-                                      precond="block_jacobi", rtol=rtol, sample=max(1, len(probs) // 4))
+                                      precond=args.batch_precond, rtol=rtol, sample=max(1, len(probs) // 4))
     t_tune = time.perf_counter() - t0
 
     def run_batch():
         return bt.solve(1.0, nus, fixed, vals, plane="strain", precision="mixed",
-                        precond="block_jacobi", rtol=rtol)
+                        precond=args.batch_precond, rtol=rtol)
 
     for _ in range(args.warmup):
         u, st = run_batch()
@@ -575,8 +577,10 @@ def batch_leg(args, pkg, ctx, stream, dist):
         errs.append(float(np.linalg.norm(parts[k] - ref) / np.linalg.norm(ref)))
     bt.close()
     its = np.array([s["iterations"] for s in st])
+    pc = "geometric-multigrid" if args.batch_precond == "multigrid" else "block-Jacobi"
     return {"workload": f"{len(probs)} plane-strain Q1 quad meshes, n ~ U{{16..256}}, mixed "
-                        f"block-Jacobi PCG to {rtol:g}, one persistent launch",
+                        f"{pc} PCG to {rtol:g}, one persistent launch",
+            "precond": args.batch_precond,
             "n_dof_total": n_total, "value": value, "unit": UNIT, "ms_per_batch": ms,
             "setup_s": t_setup, "autotune_s": t_tune, "launch": shape,
             "statuses_ok": int(sum(s["status"] == 0 for s in st)),

@@ -52,13 +52,18 @@ struct sfem_batch {
     int64_t big_nodes = 16384;           // meshes with at least this many nodes use a cluster
     int last_grid = 0, last_cluster = 0;
     std::vector<int64_t> h_nodes;        // nodes per mesh
+    // multigrid (built at the first multigrid solve): structured meshes get a hierarchy
+    bool mg_checked = false, mg_any = false;
+    std::vector<int> h_mg_ne;            // elements per direction of each structured mesh, else 0
+    char *mg_buf = nullptr;              // every hierarchy's arrays
+    MgMesh *mg_rec = nullptr;            // device: one record per mesh (nlev 0: no hierarchy)
 };
 
 namespace {
 
 using namespace sfem_dev;
 
-template <int NDIM, int NEN, int NGP, int B, bool MIXED>
+template <int NDIM, int NEN, int NGP, int B, bool MIXED, bool MG>
 __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
     __shared__ double red[128];  // two halves, alternating (block_sum2)
     __shared__ double xch[4];
@@ -74,7 +79,8 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = *cl.map_shared_rank(&s_mesh, 0);
         cl.sync();
         if (q >= a.nbig) break;
-        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED, UF, WF>(ClusterGroup(), tab, a, a.order[q], red, xch, &s_flag);
+        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED, UF, WF, 1, false, false, MG>(ClusterGroup(), tab, a,
+                                                                                       a.order[q], red, xch, &s_flag);
         cl.sync();
     }
     // 2. small meshes: every CTA on its own
@@ -84,7 +90,8 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = (int64_t)a.nbig + s_mesh;
         __syncthreads();
         if (q >= a.nmesh) break;
-        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED, UF, WF>(SoloGroup(), tab, a, a.order[q], red, xch, &s_flag);
+        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED, UF, WF, 1, false, false, MG>(SoloGroup(), tab, a,
+                                                                                    a.order[q], red, xch, &s_flag);
         __syncthreads();
     }
     cl.sync();  // peers may still read this CTA's shared memory until every CTA is done
@@ -142,13 +149,34 @@ __global__ void k_batch_elems(const int64_t *__restrict__ IENin, int64_t total_e
     IENc[t] = pad_base[lo] + v;  // 1-based combined node id
 }
 
-template <int NDIM, int NEN, int NGP, int B, bool MIXED>
+// Structured-grid check of every mesh of a batch: ok[m] is cleared when an
+// element of mesh m differs from the meshgrid connectivity of cand[m]
+// elements per direction (combined 0-based node ids, element index fastest).
+__global__ void k_mg_check(const int *__restrict__ ien, int64_t nEl, int nen, int ndim,
+                           const BatchMesh *__restrict__ meshes, int64_t nmesh, const int *__restrict__ cand,
+                           int *__restrict__ ok) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nEl) return;
+    int64_t lo = 0, hi = nmesh - 1;  // last mesh with elem0 <= e
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (meshes[mid].elem0 <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    const BatchMesh M = meshes[lo];
+    const int ne = cand[lo];
+    if (ne == 0 || e >= M.elem1) return;
+    for (int c = 0; c < nen; ++c)
+        if ((int64_t)ien[(int64_t)c * nEl + e] != M.node0 + mg_grid_node(ndim, ne, e - M.elem0, c) - 1) ok[lo] = 0;
+}
+
+template <int NDIM, int NEN, int NGP, int B, bool MIXED, bool MG = false>
 int launch_batch(sfem_ctx *ctx, sfem_batch *bt, const BatchArgs &args) {
     constexpr int GS = NEN * NDIM + 1;
     const int threads = bt->threads;
     const int ngroups = (threads / 32) / NGP;
     const size_t smem = sizeof(double) * (size_t)ngroups * (NGP * 32 * GS + NGP * 32);
-    auto kern = k_batch<NDIM, NEN, NGP, B, MIXED>;
+    auto kern = k_batch<NDIM, NEN, NGP, B, MIXED, MG>;
     SFEM_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const ElemTableB tab = make_table_b(NDIM, bt->fclass);
     SFEM_CUDA(ctx, cudaMemsetAsync(bt->queue, 0, 2 * sizeof(unsigned), ctx->stream));
@@ -194,6 +222,15 @@ int launch_batch(sfem_ctx *ctx, sfem_batch *bt, const BatchArgs &args) {
 
 template <bool MIXED>
 int dispatch_batch(sfem_ctx *ctx, sfem_batch *bt, const BatchArgs &args) {
+    if constexpr (MIXED) {
+        if (args.mg && bt->fclass == SFEM_Q1) {  // the multigrid variants (Q1 classes, mixed precision)
+            if (bt->ndim == 2)
+                return bt->b == 1 ? launch_batch<2, 4, 4, 1, true, true>(ctx, bt, args)
+                                  : launch_batch<2, 4, 4, 2, true, true>(ctx, bt, args);
+            return bt->b == 1 ? launch_batch<3, 8, 8, 1, true, true>(ctx, bt, args)
+                              : launch_batch<3, 8, 8, 3, true, true>(ctx, bt, args);
+        }
+    }
     if (bt->fclass == SFEM_Q2) return launch_batch<2, 9, 4, 1, MIXED>(ctx, bt, args);
     if (bt->ndim == 2)
         return bt->b == 1 ? launch_batch<2, 4, 4, 1, MIXED>(ctx, bt, args) : launch_batch<2, 4, 4, 2, MIXED>(ctx, bt, args);
@@ -373,6 +410,71 @@ static int batch_buffers(sfem_ctx *ctx, sfem_batch *bt) {
     return SFEM_OK;
 }
 
+// Multigrid hierarchies of the batch's structured meshes (once per batch):
+// the connectivity check on the device, then one buffer for every
+// hierarchy.  The fine level's vectors and smoother are indexed by combined
+// node like the CG's, so their pointers are shifted by the mesh's first node.
+static int batch_mg(sfem_ctx *ctx, sfem_batch *bt) {
+    if (bt->mg_checked) return SFEM_OK;
+    const int64_t nm = bt->nmesh;
+    const int b = bt->b;
+    std::vector<int> cand(nm, 0), ok(nm, 1);
+    bool anyc = false;
+    for (int64_t m = 0; m < nm; ++m) {
+        if (bt->fclass != SFEM_Q1) break;
+        const int ne = mg_grid_ne(bt->ndim, bt->h_node_off[m + 1] - bt->h_node_off[m],
+                                  bt->h_elem_off[m + 1] - bt->h_elem_off[m]);
+        cand[m] = mg_levels(ne) >= 2 ? ne : 0;
+        anyc = anyc || cand[m] > 0;
+    }
+    if (anyc) {
+        int *dc = nullptr, *dok = nullptr;
+        int st = sfem_dalloc(ctx, (void **)&dc, sizeof(int) * nm, "multigrid check");
+        if (st == SFEM_OK) st = sfem_dalloc(ctx, (void **)&dok, sizeof(int) * nm, "multigrid check");
+        if (st == SFEM_OK) st = sfem_copy_in(ctx, dc, cand.data(), sizeof(int) * nm, SFEM_MEM_HOST);
+        if (st == SFEM_OK) st = sfem_copy_in(ctx, dok, ok.data(), sizeof(int) * nm, SFEM_MEM_HOST);
+        if (st == SFEM_OK && bt->mesh->nEl > 0) {
+            k_mg_check<<<(unsigned)sfem_cdiv(bt->mesh->nEl, 256), 256, 0, ctx->stream>>>(
+                bt->mesh->ien, bt->mesh->nEl, bt->nen, bt->ndim, bt->meshes, nm, dc, dok);
+            SFEM_LAUNCHED(ctx);
+        }
+        if (st == SFEM_OK) st = sfem_copy_out(ctx, ok.data(), dok, sizeof(int) * nm, SFEM_MEM_HOST);
+        sfem_dfree(ctx, dc);
+        sfem_dfree(ctx, dok);
+        SFEM_TRY(st);
+    }
+    bt->h_mg_ne.assign(nm, 0);
+    std::vector<int64_t> off(nm + 1, 0);
+    for (int64_t m = 0; m < nm; ++m) {
+        int64_t bytes = 0;
+        if (cand[m] > 0 && ok[m]) {
+            bt->h_mg_ne[m] = cand[m];
+            bytes = (mg_layout(bt->ndim, b, cand[m], (bt->h_pad_base[m + 1] - bt->h_pad_base[m]) * b, nullptr,
+                               nullptr) + 255) / 256 * 256;
+            bt->mg_any = true;
+        }
+        off[m + 1] = off[m] + bytes;
+    }
+    std::vector<MgMesh> rec(nm);
+    memset(rec.data(), 0, sizeof(MgMesh) * nm);
+    if (bt->mg_any) {
+        SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->mg_buf, (size_t)off[nm], "batch multigrid"));
+        for (int64_t m = 0; m < nm; ++m) {
+            if (!bt->h_mg_ne[m]) continue;
+            const int64_t padded = bt->h_pad_base[m + 1] - bt->h_pad_base[m], node0 = bt->h_pad_base[m];
+            mg_layout(bt->ndim, b, bt->h_mg_ne[m], padded * b, bt->mg_buf + off[m], &rec[m]);
+            MgLevel &f = rec[m].lev[0];
+            f.x = (float *)((uintptr_t)f.x - sizeof(float) * node0 * b);
+            f.t = (float *)((uintptr_t)f.t - sizeof(float) * node0 * b);
+            f.minv = (float *)((uintptr_t)f.minv - sizeof(float) * node0 * b * b);
+        }
+    }
+    SFEM_TRY(sfem_dalloc(ctx, (void **)&bt->mg_rec, sizeof(MgMesh) * nm, "batch multigrid records"));
+    SFEM_TRY(sfem_copy_in(ctx, bt->mg_rec, rec.data(), sizeof(MgMesh) * nm, SFEM_MEM_HOST));
+    bt->mg_checked = true;
+    return SFEM_OK;
+}
+
 static int grow(sfem_ctx *ctx, void **p, int64_t *cap, int64_t need, size_t elem, const char *what) {
     if (need <= *cap && *p) return SFEM_OK;
     sfem_dfree(ctx, *p);
@@ -474,7 +576,11 @@ static int batch_run(sfem_ctx *ctx, sfem_batch *bt, const sfem_solve_opts &o, in
     a.rtol = o.rtol;
     a.delta2 = o.reliable_delta * o.reliable_delta;
     a.maxit = o.maxit > 0 ? o.maxit : 1000000;
-    a.block_jacobi = o.precond == SFEM_PC_BLOCK_JACOBI ? 1 : 0;
+    a.block_jacobi = o.precond != SFEM_PC_JACOBI ? 1 : 0;
+    if (o.precond == SFEM_PC_MULTIGRID && o.precision == SFEM_MIXED) {
+        SFEM_TRY(batch_mg(ctx, bt));
+        if (bt->mg_any) a.mg = bt->mg_rec;
+    }
     a.stats = dstats;
     a.err = ctx->d_err;
     a.nmesh_all = bt->nmesh;
@@ -485,7 +591,7 @@ static int batch_opts(sfem_ctx *ctx, const sfem_solve_opts *opts, sfem_solve_opt
     sfem_solve_opts_default(o);
     if (opts) *o = *opts;
     if (!(o->rtol >= 0.0) || o->maxit < 0 || (o->precision != SFEM_FP64 && o->precision != SFEM_MIXED) ||
-        (o->precond != SFEM_PC_JACOBI && o->precond != SFEM_PC_BLOCK_JACOBI) ||
+        o->precond < SFEM_PC_JACOBI || o->precond > SFEM_PC_MULTIGRID ||
         !(o->reliable_delta > 0.0 && o->reliable_delta < 1.0))
         return sfem_set_error(ctx, SFEM_BAD_ARG, "bad solve options");
     return SFEM_OK;
@@ -601,7 +707,7 @@ extern "C" int sfem_batch_destroy(sfem_batch *bt) {
     cudaSetDevice(ctx->device);
     void *bufs[] = {bt->meshes, bt->order, bt->queue, bt->kbuf, bt->val64, bt->val32, bt->ud, bt->b64, bt->x64,
                     bt->q64, bt->vecT, bt->fixed, bt->gfixed, bt->E, bt->nu, bt->fvals, bt->u, bt->fdofs,
-                    bt->fix_off_dev};
+                    bt->fix_off_dev, bt->mg_buf, bt->mg_rec};
     for (void *p : bufs) sfem_dfree(ctx, p);
     if (bt->mesh) sfem_mesh_release(bt->mesh);
     cudaStreamSynchronize(ctx->stream);

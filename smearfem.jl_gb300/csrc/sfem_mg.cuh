@@ -102,6 +102,46 @@ inline int64_t mg_layout(int ndim, int B, int ne, int64_t ndp, char *base, MgMes
     return off;
 }
 
+// Candidate elements per direction of a mesh with nN nodes and nEl
+// elements: ne with ne^ndim == nEl and (ne + 1)^ndim == nN, else 0.
+inline int mg_grid_ne(int ndim, int64_t nN, int64_t nEl) {
+    auto ipow = [](int64_t b, int e) {
+        int64_t r = 1;
+        for (int i = 0; i < e; ++i) r *= b;
+        return r;
+    };
+    int64_t ne = 1;
+    while (ipow(ne, ndim) < nEl && ne < (1 << 20)) ++ne;
+    return (ipow(ne, ndim) == nEl && ipow(ne + 1, ndim) == nN) ? (int)ne : 0;
+}
+
+// Node c (1-based) of structured element e of an ne^ndim grid, the
+// reference's meshgrid connectivity (examples/vector3D.jl:76-101).
+__host__ __device__ inline int64_t mg_grid_node(int ndim, int64_t ne, int64_t e, int c) {
+    const int64_t n1 = ne + 1, p = n1 * n1;
+    const int64_t i = e % ne, j = (e / ne) % ne, k = e / (ne * ne);
+    if (ndim == 2) {
+        const int64_t lo = j * n1 + i + 1, hi = (j + 1) * n1 + i + 1;
+        return c == 0 ? lo : (c == 1 ? lo + 1 : (c == 2 ? hi + 1 : hi));
+    }
+    const int64_t base = k * p + j * n1 + i + 1 + (c >= 4 ? p : 0);
+    const int q = c & 3;
+    return q == 0 ? base : (q == 1 ? base + 1 : (q == 2 ? base + n1 + 1 : base + n1));
+}
+
+// Elements per direction when the mesh is the reference's structured grid
+// (nodes x fastest, Q1 connectivity as meshgrid makes it), else 0.  IEN is
+// column-major with leading dimension ld, 1-based.
+inline int mg_structured_ne(int ndim, int fclass, int nen, int64_t nN, int64_t nEl, const int64_t *IEN, int64_t ld) {
+    if (fclass != SFEM_Q1 || nen != (1 << ndim) || nEl < 1) return 0;
+    const int ne = mg_grid_ne(ndim, nN, nEl);
+    if (ne == 0) return 0;
+    for (int64_t e = 0; e < nEl; ++e)
+        for (int a = 0; a < nen; ++a)
+            if (IEN[e + a * ld] != mg_grid_node(ndim, ne, e, a)) return 0;
+    return ne;
+}
+
 namespace sfem_dev {
 
 template <int NDIM>

@@ -26,7 +26,6 @@
 // recycled buffer's old contents.
 #include <algorithm>
 #include <atomic>
-#include <cmath>
 #include <initializer_list>
 #include <chrono>
 #include <condition_variable>
@@ -329,48 +328,6 @@ int64_t request_bytes(int ndim, int nen, int b, int64_t nN, int64_t nEl, int64_t
     bytes += 2 * nd + 8 * 4 * nd + 8 * (6 * nd + nd * b);         // masks, FP64 vectors, CG vectors + minv
     bytes += 8 * b * nN * 2;                                      // u, initial guess (warm starts)
     return bytes;
-}
-
-int64_t ipow(int64_t b, int e) {
-    int64_t r = 1;
-    for (int i = 0; i < e; ++i) r *= b;
-    return r;
-}
-
-// Elements per direction when the mesh is the reference's structured grid
-// (the node numbering and Q1 connectivity of examples/vector3D.jl:66-101:
-// nodes x fastest, IEN column-major and 1-based), else 0.
-int structured_ne(int ndim, int fclass, int nen, int64_t nN, int64_t nEl, const int64_t *IEN) {
-    if (fclass != SFEM_Q1 || nen != (1 << ndim) || nEl < 1) return 0;
-    int64_t ne = 0;
-    for (int64_t c = std::max<int64_t>(1, (int64_t)std::llround(std::pow((double)nEl, 1.0 / ndim)) - 1);
-         ipow(c, ndim) <= nEl; ++c)
-        if (ipow(c, ndim) == nEl) ne = c;
-    if (ne < 1 || ne > (1 << 20) || ipow(ne + 1, ndim) != nN) return 0;
-    const int64_t n1 = ne + 1, p = n1 * n1;
-    for (int64_t e = 0; e < nEl; ++e) {
-        const int64_t i = e % ne, j = (e / ne) % ne, k = e / (ne * ne);
-        int64_t c[8];
-        if (ndim == 2) {
-            c[0] = j * n1 + i + 1;
-            c[1] = c[0] + 1;
-            c[2] = (j + 1) * n1 + i + 2;
-            c[3] = (j + 1) * n1 + i + 1;
-        } else {
-            const int64_t base = k * p + j * n1 + i + 1;
-            c[0] = base;
-            c[1] = base + 1;
-            c[2] = base + n1 + 1;
-            c[3] = base + n1;
-            c[4] = base + p;
-            c[5] = base + p + 1;
-            c[6] = base + p + n1 + 1;
-            c[7] = base + p + n1;
-        }
-        for (int a = 0; a < nen; ++a)
-            if (IEN[e + a * nEl] != c[a]) return 0;
-    }
-    return (int)ne;
 }
 
 // Dynamic shared memory of process_mesh for one class at `threads` per CTA.
@@ -861,7 +818,7 @@ extern "C" int sfem_server_submit(sfem_server *s, int ndim, int function_class, 
         r->IEN.assign(IEN, IEN + nEl * nen);
         if (b > 1) r->ID.assign(ID, ID + nNodes * b);
         if (want_mg) {
-            const int ne = structured_ne(ndim, function_class, nen, nNodes, nEl, IEN);
+            const int ne = mg_structured_ne(ndim, function_class, nen, nNodes, nEl, IEN, nEl);
             r->mg_ne = mg_levels(ne) >= 2 ? ne : 0;
         }
     }

@@ -1,7 +1,7 @@
-"""GPU: the geometric multigrid preconditioner of the serving solver
-(structured meshgrid Q1 meshes, mixed precision).
+"""GPU: the geometric multigrid preconditioner of the serving and batch
+solvers (structured meshgrid Q1 meshes, mixed precision).
 
-Each served request must match its single-mesh FP64 solve within 1e-8,
+Each served request or batch mesh must match its single-mesh FP64 solve within 1e-8,
 need far fewer iterations than block Jacobi, and stay bitwise the same
 alone and in a mix; meshes that are not the structured grid (elements
 renumbered) fall back to block Jacobi and stay correct.
@@ -116,3 +116,51 @@ def test_multigrid_needs_mixed_precision_and_known_option(sfem):
     with sfem.Server(cluster=2, rtol=1e-12, precision="fp64", precond="multigrid") as srv:
         u, res = srv.wait(_submit(srv, p), timeout_ms=60000)
     assert res["status"] == 0
+
+
+def _batch(sfem, ctx, probs, precond, launch=None, E=None):
+    bt = sfem.Batch.from_problems(probs, ctx=ctx)
+    if launch:
+        bt.set_launch(*launch)
+    Ev = 1.0 if E is None else E
+    u, st = bt.solve(Ev, np.array([float(p.nu[0]) for p in probs]), [p.fixed_dofs for p in probs],
+                     [p.fixed_vals for p in probs], plane=probs[0].plane, precision="mixed",
+                     precond=precond, rtol=1e-12)
+    parts = bt.split(u)
+    bt.close()
+    return parts, st
+
+
+def _unit_E(p):
+    p.Young = np.ones(1)
+    return p
+
+
+@pytest.mark.timeout(600)
+@pytest.mark.parametrize("launch", [None, (512, 1, 4, 1)])
+def test_batch_multigrid_matches_single_mesh_solves(sfem, ctx, launch):
+    """Meshes on one CTA each (default shape) or on 4-CTA clusters; a mesh
+    too small for a hierarchy (ne = 2) is solved with block Jacobi."""
+    mg = sfem.meshgen
+    rng = np.random.default_rng(4)
+    probs = [mg.quad_problem(n, 4, jitter=0.15, nu_range=(0.25, 0.45), plane="strain", rtol=1e-10, rng=rng)
+             for n in (2, 17, 40, 9, 64, 33)]
+    parts, st = _batch(sfem, ctx, probs, "multigrid", launch)
+    _, stb = _batch(sfem, ctx, probs, "block_jacobi", launch)
+    for p, u, s, sb in zip(probs, parts, st, stb):
+        assert s["status"] == 0, (p.name, s)
+        assert _rel(u, _single(sfem, ctx, p)) <= TOL_U, (p.name, s)
+        if p.ne >= 17:
+            assert s["iterations"] * 5 < sb["iterations"], (p.name, s["iterations"], sb["iterations"])
+
+
+@pytest.mark.timeout(600)
+def test_batch_multigrid_hexes_and_determinism(sfem, ctx):
+    mg = sfem.meshgen
+    probs = [_unit_E(mg.hex_problem(n, 60 + n, jitter=0.2, nu=0.35, top="modes")) for n in (5, 12, 9)]
+    parts, st = _batch(sfem, ctx, probs, "multigrid")
+    for p, u, s in zip(probs, parts, st):
+        assert s["status"] == 0 and s["iterations"] < 80, (p.name, s)
+        assert _rel(u, _single(sfem, ctx, p)) <= TOL_U, (p.name, s)
+    alone, _ = _batch(sfem, ctx, [probs[1]], "multigrid")
+    assert np.array_equal(alone[0], parts[1])
