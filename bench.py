@@ -70,7 +70,7 @@ def parse_args(argv=None):
     ap.add_argument("--batch-precond", default="multigrid", choices=["multigrid", "block_jacobi"],
                     help="batch-leg preconditioner (multigrid: structured meshes)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
-    ap.add_argument("--serve-requests", type=int, default=240, help="requests in the saturating stream")
+    ap.add_argument("--serve-requests", type=int, default=960, help="requests in the saturating stream")
     ap.add_argument("--serve-pool", type=int, default=96, help="distinct meshes the stream draws from")
     ap.add_argument("--serve-precond", default="multigrid", choices=["multigrid", "block_jacobi"],
                     help="serving preconditioner (multigrid: structured meshes, cached per topology)")
@@ -643,19 +643,26 @@ def _sustained(recs, ndof_of):
     return len(done) / win, sum(ndof_of(k) for k, _ in done) / win
 
 
-def _cg_iteration_bytes(p):
+def _cg_iteration_bytes(p, mg=False):
     """Algorithmic memory traffic of one FP32 CG iteration of the per-mesh
     solver on structured mesh p: every stored b x b block of K and its column
     index once ((3 ne + 1)^ndim blocks), plus per DOF the SpMV's own-row reads
     of p and z, writes of the new p and of q and the fixed flag (17 B), and the
     update's reads of x, r, p, q and the nodal inverse and writes of x, r, z
-    (28 + 4 b B)."""
+    (28 + 4 b B).  With the multigrid V(1,1) cycle: the fine level's residual
+    and smoothing products (K twice, 38 + 4 b B per DOF of vectors, the
+    restriction and the prolongation), and the coarse levels, each 2^ndim
+    times smaller, on top."""
     b = p.ndim
     nnzb = (3 * p.ne + 1) ** b
-    return nnzb * (4 * b * b + 4) + p.n_dof * (17 + 28 + 4 * b)
+    kb = nnzb * (4 * b * b + 4)
+    cg = kb + p.n_dof * (17 + 28 + 4 * b)
+    if not mg:
+        return cg
+    return cg + (2 * kb + p.n_dof * (38 + 4 * b)) * 2 ** b / (2 ** b - 1)
 
 
-def _window_traffic(recs, pool):
+def _window_traffic(recs, pool, mg):
     """Memory traffic rate of the CG iterations over the saturated window
     (the requests _sustained counts) and the share of group time per class."""
     claims = [r["t_claim_ms"] for _, _, r in recs]
@@ -663,7 +670,7 @@ def _window_traffic(recs, pool):
     done = [(k, r) for k, _, r in recs if t0 < r["t_end_ms"] <= t1]
     if t1 <= t0 or not done:
         return None
-    nbytes = sum(r["iterations"] * _cg_iteration_bytes(pool[k]) for k, r in done)
+    nbytes = sum(r["iterations"] * _cg_iteration_bytes(pool[k], mg and pool[k].ne >= 3) for k, r in done)
     gt = {2: 0.0, 3: 0.0}
     its = {2: [], 3: []}
     for k, _, r in recs:
@@ -714,7 +721,7 @@ def serve_leg(args, pkg, ctx, dist):
         same = sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs)
         capacity = n / wall
         sus_rps, sus_dps = _sustained(recs, lambda k: pool[k].n_dof)
-        traffic = _window_traffic(recs, pool)
+        traffic = _window_traffic(recs, pool, args.serve_precond == "multigrid")
         peak = srv.info()
         # below capacity: latency without a backlog
         m = max(20, min(120, int(capacity * 8)))
@@ -763,8 +770,9 @@ def serve_leg(args, pkg, ctx, dist):
             "gpu_concurrency": _concurrency(recs),
             "cg_memory": None if traffic is None else {
                 "achieved_gbs": traffic["gbs"], "frac_hbm": traffic["gbs"] / measured_peaks()[0],
-                "basis": "iterations x (K blocks + column indices + 11 FP32 vectors per DOF) of the "
-                         "requests finished in the saturated window, over that window",
+                "basis": "iterations x (K blocks + column indices + 11 FP32 vectors per DOF, and with "
+                         "multigrid the V(1,1) cycle's two fine products and vectors plus coarse levels) of "
+                         "the requests finished in the saturated window, over that window; set-up not counted",
                 "group_time_share": traffic["group_time_share"],
                 "iterations_median": traffic["iterations_median"]},
             "rel_err_max_sample": max(errs),
