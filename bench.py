@@ -416,6 +416,14 @@ def our_arm(args, dist):
                                     "launch_ms": spmv32_ms, "algorithmic_bytes_per_launch": sym_bytes,
                                     "achieved_gbs": sym_bytes / (spmv32_ms * 1e-3) / 1e9,
                                     "frac_hbm": sym_bytes / (spmv32_ms * 1e-3) / 1e9 / hbm_peak}}
+        # the same mixed solve with the geometric multigrid preconditioner (structured mesh)
+        msg, infg, _ = timed(lambda: step(precision="mixed", precond="multigrid"), args.steps, args.warmup)
+        vmg, msg = aggregate(dist, n_dof, msg)
+        line["mixed"]["multigrid"] = {
+            "value": vmg, "ms_per_step": msg, "iterations": infg[-1]["iterations"],
+            "fp64_refreshes": infg[-1]["reliable_updates"], "relres": infg[-1]["relres"], "rel_err": rel_err(dU),
+            "speedup_vs_fp64": (line["ms_per_step"] / msg) if "ms_per_step" in line else None,
+            "solve_s": infg[-1]["solve_s"]}
     if "e2e" in args.legs:
         # ---- e2e: C ABI with pinned host buffers, copies inside the timed region
         def pinned(a):

@@ -64,6 +64,7 @@ struct sfem_mesh {
     int *col = nullptr;
     int *g2i = nullptr;
     unsigned long long neg_det = 0;
+    int mg_ne = -1;  // elements per direction of a structured (meshgrid) mesh, 0 if not, -1 unknown
 };
 
 struct sfem_matrix {

@@ -13,7 +13,7 @@
 // fine DOF is, so P' = diag(free_f) P diag(free_c).
 //
 // Coarse operators are Galerkin products A_{l+1} = P'^T A_l P' with A_0 the
-// masked FP32 K.  Their node pattern is again the 3^ndim neighbourhood, so
+// masked K rounded to FP32.  Their node pattern is again the 3^ndim neighbourhood, so
 // they are stored as stencils: block (I, I + offset s) at
 // A[(s * B*B + e) * nnode + I], zero where the neighbour is off the grid.
 //
@@ -182,8 +182,8 @@ __device__ __forceinline__ void mg_free(const BatchArgs &a, const BatchMesh &M, 
     for (int c = 0; c < B; ++c) f[c] = l == 0 ? a.fixed[(M.node0 + li) * B + c] == 0 : L.fr[li * B + c] != 0;
 }
 
-// Block A_l(i, j) of neighbours i, j on level l: the sliced-ELL FP32 K on
-// the fine level (the position of j among i's ascending neighbours follows
+// Block A_l(i, j) of neighbours i, j on level l: the sliced-ELL K (FP64,
+// rounded to FP32) on the fine level (the position of j among i's ascending neighbours follows
 // from the grid), the stencil on coarse levels.  False when the fine
 // pattern is not the structured one.
 template <int NDIM, int B>
@@ -203,7 +203,7 @@ __device__ __forceinline__ bool mg_block(const BatchArgs &a, const BatchMesh &M,
         const int64_t slab = a.sliceptr[r >> 5] + pos;
         if (pos >= a.rowlen[r] || a.col[slab * 32 + lane] != (int)(M.node0 + mg_index<NDIM>(cj, L.n))) return false;
 #pragma unroll
-        for (int e = 0; e < B * B; ++e) blk[e] = a.val32[v32_at<B>(slab, lane, e)];
+        for (int e = 0; e < B * B; ++e) blk[e] = (float)a.val64[(slab * B * B + e) * 32 + lane];
     } else {
         const int s = mg_stencil<NDIM>(ci, cj);
 #pragma unroll
@@ -253,228 +253,266 @@ __device__ __forceinline__ bool mg_inv_block(const double *Din, const bool *f, d
     return true;
 }
 
-// Hierarchy set-up after K (FP64 and FP32), the Dirichlet mask and the
-// block-Jacobi inverse `bj` (FP32, [node][B][B]) are in place.  Returns
-// through *flag (group-shared) SFEM_SINGULAR or SFEM_BAD_INDEX on failure.
+// ---- hierarchy set-up, pass by pass.  Each pass is a loop over (gt, gstride)
+// that the group driver below (mg_setup) and the grid-wide kernels of the
+// single-mesh solver share; a barrier separates consecutive passes.  Failures
+// go to *flag (SFEM_SINGULAR, SFEM_BAD_INDEX) by atomicMax.
+
+// Fine level: W D^-1 from the block-Jacobi inverse `bj` (FP32, [node][B][B])
+// and the node's row of K.
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_pass_fine(const BatchArgs &a, const BatchMesh &M, const MgLevel &F,
+                                             const float *bj, int64_t gt, int64_t gstride) {
+    for (int64_t li = gt; li < F.nnode; li += gstride) {
+        const int64_t r = M.node0 + li;
+        float Di[B * B];
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) Di[e] = bj[r * B * B + e];
+        float rs[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) rs[i] = 0.0f;
+        const int len = a.rowlen[r];
+        const int64_t slab0 = a.sliceptr[r >> 5];
+        const int lane = (int)(r & 31);
+        for (int k = 0; k < len; ++k) {
+            const int64_t slab = slab0 + k;
+            const int c = a.col[slab * 32 + lane];
+            float blk[B * B];
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) blk[e] = (float)a.val64[(slab * B * B + e) * 32 + lane];
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) {
+                    if (a.fixed[(int64_t)c * B + j]) continue;
+                    float v = 0.0f;
+#pragma unroll
+                    for (int m = 0; m < B; ++m) v = fmaf(Di[i * B + m], blk[m * B + j], v);
+                    rs[i] += fabsf(v);
+                }
+        }
+        float rho = 0.0f;
+#pragma unroll
+        for (int i = 0; i < B; ++i) rho = fmaxf(rho, rs[i]);
+        const float w = rho > 0.0f ? (4.0f / 3.0f) / rho : 0.0f;
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) F.minv[r * B * B + e] = w * Di[e];
+    }
+}
+
+// Coarse free flags: the coinciding fine DOF's.
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_pass_free(const BatchArgs &a, const BatchMesh &M, const MgLevel &F,
+                                             const MgLevel &C, int l, int64_t gt, int64_t gstride) {
+    for (int64_t I = gt; I < C.nnode; I += gstride) {
+        int cI[3], cf[3] = {0, 0, 0};
+        mg_coords<NDIM>(I, C.n, cI);
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) cf[d] = min(2 * cI[d], F.n);
+        bool f[B];
+        mg_free<NDIM, B>(a, M, F, l, cf, f);
+#pragma unroll
+        for (int c = 0; c < B; ++c) C.fr[I * B + c] = f[c] ? 1 : 0;
+    }
+}
+
+// Galerkin product: one (coarse node, stencil neighbour) block per step.
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_pass_galerkin(const BatchArgs &a, const BatchMesh &M, const MgLevel &F,
+                                                 const MgLevel &C, int l, int64_t gt, int64_t gstride, int *flag) {
+    constexpr int S = NDIM == 2 ? 9 : 27;
+    const int64_t total = (int64_t)C.nnode * S;
+    for (int64_t q = gt; q < total; q += gstride) {
+        const int64_t I = q % C.nnode;
+        const int s = (int)(q / C.nnode);
+        int cI[3], cJ[3] = {0, 0, 0};
+        mg_coords<NDIM>(I, C.n, cI);
+        const int off[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+        bool valid = true;
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) {
+            cJ[d] = cI[d] + off[d];
+            valid = valid && cJ[d] >= 0 && cJ[d] <= C.n;
+        }
+        float acc[B * B];
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) acc[e] = 0.0f;
+        if (valid) {
+            // per direction: fine pairs (i, j), i in supp(I), j in supp(J), |i - j| <= 1
+            int pi[3][7], pj[3][7], np[3] = {1, 1, 1};
+            float pw[3][7];
+            pi[2][0] = pj[2][0] = 0;
+            pw[2][0] = 1.0f;
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) {
+                int k = 0;
+                const int ccI = min(2 * cI[d], F.n);
+                for (int i = ccI - 1; i <= ccI + 1; ++i) {
+                    if (i < 0 || i > F.n) continue;
+                    const float wi = mg_w1(i, cI[d], F.n);
+                    if (wi == 0.0f) continue;
+                    for (int j = i - 1; j <= i + 1; ++j) {
+                        if (j < 0 || j > F.n) continue;
+                        const float wj = mg_w1(j, cJ[d], F.n);
+                        if (wj == 0.0f) continue;
+                        pi[d][k] = i;
+                        pj[d][k] = j;
+                        pw[d][k] = wi * wj;
+                        ++k;
+                    }
+                }
+                np[d] = k;
+            }
+            for (int kz = 0; kz < np[2]; ++kz)
+                for (int ky = 0; ky < np[1]; ++ky)
+                    for (int kx = 0; kx < np[0]; ++kx) {
+                        const int ci[3] = {pi[0][kx], pi[1][ky], pi[2][kz]};
+                        const int cj[3] = {pj[0][kx], pj[1][ky], pj[2][kz]};
+                        const float w = pw[0][kx] * pw[1][ky] * pw[2][kz];
+                        float blk[B * B];
+                        if (!mg_block<NDIM, B>(a, M, F, l, ci, cj, blk)) {
+                            atomicMax(flag, (int)SFEM_BAD_INDEX);
+                            continue;
+                        }
+                        bool fi[B], fj[B];
+                        mg_free<NDIM, B>(a, M, F, l, ci, fi);
+                        mg_free<NDIM, B>(a, M, F, l, cj, fj);
+#pragma unroll
+                        for (int i = 0; i < B; ++i)
+#pragma unroll
+                            for (int j = 0; j < B; ++j)
+                                if (fi[i] && fj[j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
+                    }
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j)
+                    if (!C.fr[I * B + i] || !C.fr[mg_index<NDIM>(cJ, C.n) * B + j]) acc[i * B + j] = 0.0f;
+        }
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) C.A[((int64_t)s * B * B + e) * C.nnode + I] = acc[e];
+    }
+}
+
+// Smoother of a coarse level: W D^-1 from its stencil's centre block and rows.
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_pass_smoother(const MgLevel &C, int64_t gt, int64_t gstride, int *flag) {
+    constexpr int S = NDIM == 2 ? 9 : 27;
+    for (int64_t I = gt; I < C.nnode; I += gstride) {
+        double D[B * B], Di[B * B];
+        bool f[B];
+#pragma unroll
+        for (int c = 0; c < B; ++c) f[c] = C.fr[I * B + c] != 0;
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) D[e] = C.A[((int64_t)(S / 2) * B * B + e) * C.nnode + I];
+        if (!mg_inv_block<B>(D, f, Di)) {
+            atomicMax(flag, (int)SFEM_SINGULAR);
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) Di[e] = 0.0;
+        }
+        float rs[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) rs[i] = 0.0f;
+        for (int s = 0; s < S; ++s) {
+            float blk[B * B];
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) blk[e] = C.A[((int64_t)s * B * B + e) * C.nnode + I];
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) {
+                    float v = 0.0f;
+#pragma unroll
+                    for (int m = 0; m < B; ++m) v = fmaf((float)Di[i * B + m], blk[m * B + j], v);
+                    rs[i] += fabsf(v);
+                }
+        }
+        float rho = 0.0f;
+#pragma unroll
+        for (int i = 0; i < B; ++i) rho = fmaxf(rho, rs[i]);
+        const float w = rho > 0.0f ? (4.0f / 3.0f) / rho : 0.0f;
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) C.minv[I * B * B + e] = w * (float)Di[e];
+    }
+}
+
+// Coarsest level: dense inverse by Gauss-Jordan in FP64 (SPD, no pivoting),
+// by the threads of ONE CTA (CTA barriers only).
+template <int NDIM, int B>
+__device__ __forceinline__ void mg_pass_coarsest(const MgLevel &C, int n, float *cinv, double *g, int *flag) {
+    const int w2 = 2 * n;
+    for (int q = threadIdx.x; q < n * w2; q += blockDim.x) {
+        const int r = q / w2, c = q % w2;
+        double v = 0.0;
+        if (c >= n) {
+            v = (c - n == r) ? 1.0 : 0.0;
+        } else {
+            const int I = r / B, i = r % B, J = c / B, j = c % B;
+            if (!C.fr[I * B + i] || !C.fr[J * B + j]) {
+                v = (r == c) ? 1.0 : 0.0;
+            } else {
+                int cI[3], cJ[3];
+                mg_coords<NDIM>(I, C.n, cI);
+                mg_coords<NDIM>(J, C.n, cJ);
+                bool nb = true;
+#pragma unroll
+                for (int d = 0; d < NDIM; ++d) nb = nb && abs(cI[d] - cJ[d]) <= 1;
+                if (nb) v = C.A[((int64_t)mg_stencil<NDIM>(cI, cJ) * B * B + i * B + j) * C.nnode + I];
+            }
+        }
+        g[q] = v;
+    }
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        const double piv = g[k * w2 + k];
+        __syncthreads();  // every thread has the pivot before row k changes
+        if (!(piv > 0.0)) {
+            if (threadIdx.x == 0) atomicMax(flag, (int)SFEM_SINGULAR);
+            break;
+        }
+        for (int c = threadIdx.x; c < w2; c += blockDim.x) g[k * w2 + c] /= piv;
+        __syncthreads();
+        for (int q = threadIdx.x; q < n * w2; q += blockDim.x) {
+            const int r = q / w2, c = q % w2;
+            if (r == k || c == k) continue;  // column k is not read again
+            g[q] -= g[r * w2 + k] * g[k * w2 + c];
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+        const int r = q / n, c = q % n;
+        const bool fr = C.fr[(r / B) * B + r % B] && C.fr[(c / B) * B + c % B];
+        cinv[q] = fr ? (float)g[r * w2 + n + c] : 0.0f;
+    }
+}
+
+// x = C^-1 b on the coarsest level.
+__device__ __forceinline__ void mg_coarse_solve(const MgLevel &C, int n, const float *cinv, int64_t gt,
+                                                int64_t gstride) {
+    for (int64_t q = gt; q < n; q += gstride) {
+        float v = 0.0f;
+        for (int c = 0; c < n; ++c) v = fmaf(cinv[q * n + c], C.b[c], v);
+        C.x[q] = v;
+    }
+}
+
+// Hierarchy set-up by one group, after K (FP64), the Dirichlet mask and the
+// block-Jacobi inverse `bj` (FP32, [node][B][B]) are in place.
 template <class Grp, int NDIM, int B>
 __device__ __noinline__ void mg_setup(const Grp &G, const BatchArgs &a, const BatchMesh &M, const MgMesh *mgp,
                                       const float *bj, int *flag) {
-    constexpr int S = NDIM == 2 ? 9 : 27;
     const int64_t gt = (int64_t)G.rank() * blockDim.x + threadIdx.x, gstride = (int64_t)G.size() * blockDim.x;
     const int L = mgp->nlev;
-    // ---- fine level: l1-scaled inverse from the block-Jacobi inverse and the FP32 rows
-    {
-        const MgLevel F = mgp->lev[0];
-        for (int64_t li = gt; li < F.nnode; li += gstride) {
-            const int64_t r = M.node0 + li;
-            float Di[B * B];
-#pragma unroll
-            for (int e = 0; e < B * B; ++e) Di[e] = bj[r * B * B + e];
-            float rs[B];
-#pragma unroll
-            for (int i = 0; i < B; ++i) rs[i] = 0.0f;
-            const int len = a.rowlen[r];
-            const int64_t slab0 = a.sliceptr[r >> 5];
-            const int lane = (int)(r & 31);
-            for (int k = 0; k < len; ++k) {
-                const int64_t slab = slab0 + k;
-                const int c = a.col[slab * 32 + lane];
-                float blk[B * B];
-#pragma unroll
-                for (int e = 0; e < B * B; ++e) blk[e] = a.val32[v32_at<B>(slab, lane, e)];
-#pragma unroll
-                for (int i = 0; i < B; ++i)
-#pragma unroll
-                    for (int j = 0; j < B; ++j) {
-                        if (a.fixed[(int64_t)c * B + j]) continue;
-                        float s = 0.0f;
-#pragma unroll
-                        for (int m = 0; m < B; ++m) s = fmaf(Di[i * B + m], blk[m * B + j], s);
-                        rs[i] += fabsf(s);
-                    }
-            }
-            float rho = 0.0f;
-#pragma unroll
-            for (int i = 0; i < B; ++i) rho = fmaxf(rho, rs[i]);
-            const float w = rho > 0.0f ? (4.0f / 3.0f) / rho : 0.0f;
-#pragma unroll
-            for (int e = 0; e < B * B; ++e) F.minv[r * B * B + e] = w * Di[e];
-        }
-    }
-    // ---- coarse levels
+    mg_pass_fine<NDIM, B>(a, M, mgp->lev[0], bj, gt, gstride);
     for (int l = 0; l + 1 < L; ++l) {
         const MgLevel F = mgp->lev[l], C = mgp->lev[l + 1];
-        for (int64_t I = gt; I < C.nnode; I += gstride) {  // coarse free flags: the coinciding fine DOF's
-            int cI[3], cf[3] = {0, 0, 0};
-            mg_coords<NDIM>(I, C.n, cI);
-#pragma unroll
-            for (int d = 0; d < NDIM; ++d) cf[d] = min(2 * cI[d], F.n);
-            bool f[B];
-            mg_free<NDIM, B>(a, M, F, l, cf, f);
-#pragma unroll
-            for (int c = 0; c < B; ++c) C.fr[I * B + c] = f[c] ? 1 : 0;
-        }
+        mg_pass_free<NDIM, B>(a, M, F, C, l, gt, gstride);
         G.sync();
-        const int64_t total = (int64_t)C.nnode * S;
-        for (int64_t q = gt; q < total; q += gstride) {
-            const int64_t I = q % C.nnode;
-            const int s = (int)(q / C.nnode);
-            int cI[3], cJ[3] = {0, 0, 0};
-            mg_coords<NDIM>(I, C.n, cI);
-            const int off[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
-            bool valid = true;
-#pragma unroll
-            for (int d = 0; d < NDIM; ++d) {
-                cJ[d] = cI[d] + off[d];
-                valid = valid && cJ[d] >= 0 && cJ[d] <= C.n;
-            }
-            float acc[B * B];
-#pragma unroll
-            for (int e = 0; e < B * B; ++e) acc[e] = 0.0f;
-            if (valid) {
-                // per direction: fine pairs (i, j), i in supp(I), j in supp(J), |i - j| <= 1
-                int pi[3][7], pj[3][7], np[3] = {1, 1, 1};
-                float pw[3][7];
-                pi[2][0] = pj[2][0] = 0;
-                pw[2][0] = 1.0f;
-#pragma unroll
-                for (int d = 0; d < NDIM; ++d) {
-                    int k = 0;
-                    const int ccI = min(2 * cI[d], F.n);
-                    for (int i = ccI - 1; i <= ccI + 1; ++i) {
-                        if (i < 0 || i > F.n) continue;
-                        const float wi = mg_w1(i, cI[d], F.n);
-                        if (wi == 0.0f) continue;
-                        for (int j = i - 1; j <= i + 1; ++j) {
-                            if (j < 0 || j > F.n) continue;
-                            const float wj = mg_w1(j, cJ[d], F.n);
-                            if (wj == 0.0f) continue;
-                            pi[d][k] = i;
-                            pj[d][k] = j;
-                            pw[d][k] = wi * wj;
-                            ++k;
-                        }
-                    }
-                    np[d] = k;
-                }
-                for (int kz = 0; kz < np[2]; ++kz)
-                    for (int ky = 0; ky < np[1]; ++ky)
-                        for (int kx = 0; kx < np[0]; ++kx) {
-                            const int ci[3] = {pi[0][kx], pi[1][ky], pi[2][kz]};
-                            const int cj[3] = {pj[0][kx], pj[1][ky], pj[2][kz]};
-                            const float w = pw[0][kx] * pw[1][ky] * pw[2][kz];
-                            float blk[B * B];
-                            if (!mg_block<NDIM, B>(a, M, F, l, ci, cj, blk)) {
-                                atomicMax(flag, (int)SFEM_BAD_INDEX);
-                                continue;
-                            }
-                            bool fi[B], fj[B];
-                            mg_free<NDIM, B>(a, M, F, l, ci, fi);
-                            mg_free<NDIM, B>(a, M, F, l, cj, fj);
-#pragma unroll
-                            for (int i = 0; i < B; ++i)
-#pragma unroll
-                                for (int j = 0; j < B; ++j)
-                                    if (fi[i] && fj[j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
-                        }
-#pragma unroll
-                for (int i = 0; i < B; ++i)
-#pragma unroll
-                    for (int j = 0; j < B; ++j)
-                        if (!C.fr[I * B + i] || !C.fr[mg_index<NDIM>(cJ, C.n) * B + j]) acc[i * B + j] = 0.0f;
-            }
-#pragma unroll
-            for (int e = 0; e < B * B; ++e) C.A[((int64_t)s * B * B + e) * C.nnode + I] = acc[e];
-        }
+        mg_pass_galerkin<NDIM, B>(a, M, F, C, l, gt, gstride, flag);
         G.sync();
-        if (l + 2 < L) {  // smoother of the new level (the coarsest one is solved exactly)
-            for (int64_t I = gt; I < C.nnode; I += gstride) {
-                double D[B * B], Di[B * B];
-                bool f[B];
-#pragma unroll
-                for (int c = 0; c < B; ++c) f[c] = C.fr[I * B + c] != 0;
-#pragma unroll
-                for (int e = 0; e < B * B; ++e) D[e] = C.A[((int64_t)(S / 2) * B * B + e) * C.nnode + I];
-                if (!mg_inv_block<B>(D, f, Di)) {
-                    atomicMax(flag, (int)SFEM_SINGULAR);
-#pragma unroll
-                    for (int e = 0; e < B * B; ++e) Di[e] = 0.0;
-                }
-                float rs[B];
-#pragma unroll
-                for (int i = 0; i < B; ++i) rs[i] = 0.0f;
-                for (int s = 0; s < S; ++s) {
-                    float blk[B * B];
-#pragma unroll
-                    for (int e = 0; e < B * B; ++e) blk[e] = C.A[((int64_t)s * B * B + e) * C.nnode + I];
-#pragma unroll
-                    for (int i = 0; i < B; ++i)
-#pragma unroll
-                        for (int j = 0; j < B; ++j) {
-                            float v = 0.0f;
-#pragma unroll
-                            for (int m = 0; m < B; ++m) v = fmaf((float)Di[i * B + m], blk[m * B + j], v);
-                            rs[i] += fabsf(v);
-                        }
-                }
-                float rho = 0.0f;
-#pragma unroll
-                for (int i = 0; i < B; ++i) rho = fmaxf(rho, rs[i]);
-                const float w = rho > 0.0f ? (4.0f / 3.0f) / rho : 0.0f;
-#pragma unroll
-                for (int e = 0; e < B * B; ++e) C.minv[I * B * B + e] = w * (float)Di[e];
-            }
-        }
+        if (l + 2 < L) mg_pass_smoother<NDIM, B>(C, gt, gstride, flag);  // the coarsest is solved exactly
     }
-    // ---- coarsest level: dense inverse by Gauss-Jordan (one CTA; SPD, no pivoting)
-    if (G.rank() == 0) {
-        const MgLevel C = mgp->lev[L - 1];
-        const int n = mgp->ndc, w2 = 2 * n;
-        double *g = mgp->gj;
-        for (int q = threadIdx.x; q < n * w2; q += blockDim.x) {
-            const int r = q / w2, c = q % w2;
-            double v = 0.0;
-            if (c >= n) {
-                v = (c - n == r) ? 1.0 : 0.0;
-            } else {
-                const int I = r / B, i = r % B, J = c / B, j = c % B;
-                if (!C.fr[I * B + i] || !C.fr[J * B + j]) {
-                    v = (r == c) ? 1.0 : 0.0;
-                } else {
-                    int cI[3], cJ[3];
-                    mg_coords<NDIM>(I, C.n, cI);
-                    mg_coords<NDIM>(J, C.n, cJ);
-                    bool nb = true;
-#pragma unroll
-                    for (int d = 0; d < NDIM; ++d) nb = nb && abs(cI[d] - cJ[d]) <= 1;
-                    if (nb) v = C.A[((int64_t)mg_stencil<NDIM>(cI, cJ) * B * B + i * B + j) * C.nnode + I];
-                }
-            }
-            g[q] = v;
-        }
-        __syncthreads();
-        for (int k = 0; k < n; ++k) {
-            const double piv = g[k * w2 + k];
-            __syncthreads();  // every thread has the pivot before row k changes
-            if (!(piv > 0.0)) {
-                if (threadIdx.x == 0) atomicMax(flag, (int)SFEM_SINGULAR);
-                break;
-            }
-            for (int c = threadIdx.x; c < w2; c += blockDim.x) g[k * w2 + c] /= piv;
-            __syncthreads();
-            for (int q = threadIdx.x; q < n * w2; q += blockDim.x) {
-                const int r = q / w2, c = q % w2;
-                if (r == k || c == k) continue;  // column k is not read again
-                g[q] -= g[r * w2 + k] * g[k * w2 + c];
-            }
-            __syncthreads();
-        }
-        for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
-            const int r = q / n, c = q % n;
-            const bool fr = C.fr[(r / B) * B + r % B] && C.fr[(c / B) * B + c % B];
-            mgp->cinv[q] = fr ? (float)g[r * w2 + n + c] : 0.0f;
-        }
-    }
+    if (G.rank() == 0) mg_pass_coarsest<NDIM, B>(mgp->lev[L - 1], mgp->ndc, mgp->cinv, mgp->gj, flag);
     G.sync();
 }
 
@@ -653,16 +691,8 @@ __device__ __noinline__ double mg_vcycle(const Grp &G, const BatchArgs &a, const
             G.sync();
         }
     }
-    {  // coarsest: x = C^-1 b
-        const MgLevel C = mgp->lev[L - 1];
-        const int n = mgp->ndc;
-        for (int64_t q = gt; q < n; q += gstride) {
-            float v = 0.0f;
-            for (int c = 0; c < n; ++c) v = fmaf(mgp->cinv[q * n + c], C.b[c], v);
-            C.x[q] = v;
-        }
-        G.sync();
-    }
+    mg_coarse_solve(mgp->lev[L - 1], mgp->ndc, mgp->cinv, gt, gstride);  // coarsest: x = C^-1 b
+    G.sync();
     const float *xin = mgp->lev[L - 1].x;
     for (int l = L - 2; l >= 1; --l) {
         const MgLevel F = mgp->lev[l], C = mgp->lev[l + 1];

@@ -34,7 +34,7 @@
 #include <chrono>
 #include <vector>
 
-#include "sfem_internal.cuh"
+#include "sfem_meshsolve.cuh"
 
 namespace {
 
@@ -179,13 +179,18 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
 // (x = the previous direction), formed on the fly from the gathered entries;
 // each lane stores its own rows of p to pout.  This replaces the separate
 // direction update (one pass over three vectors per iteration).
-template <typename T, int B, int MODE, bool FUSE = false>
+// EPI (multigrid V-cycle on the fine level): SPMV_RES stores y = bv - K x,
+// SPMV_SMOOTH stores y = x + Mv (bv - K x) (Mv: the smoother's b x b blocks)
+// and, with MODE 3, reduces bv.y into rz and sets beta = rz / rz_prev.
+// Both skip once the solve is done.
+template <typename T, int B, int MODE, bool FUSE = false, int EPI = sfem_dev::SPMV_Y>
 __global__ void __launch_bounds__(SPMV_T)
 k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, const T *__restrict__ valU,
            const int64_t *__restrict__ sptrL, const int2 *__restrict__ lo, int64_t nN, int64_t nslices,
            const T *__restrict__ x, T *__restrict__ y, const unsigned char *__restrict__ fixed, CgScalars *S,
-           double *partial, const T *__restrict__ z = nullptr, T *__restrict__ pout = nullptr) {
-    if (MODE == 1 && S->done) return;
+           double *partial, const T *__restrict__ z = nullptr, T *__restrict__ pout = nullptr,
+           const T *__restrict__ bv = nullptr, const T *__restrict__ Mv = nullptr) {
+    if ((MODE == 1 || MODE == 3 || EPI != sfem_dev::SPMV_Y) && S->done) return;
     const T beta = FUSE ? (T)S->beta : T(0);
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -240,18 +245,43 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
             }
         }
         if (r < nN) {
+            if constexpr (EPI == sfem_dev::SPMV_Y) {
 #pragma unroll
-            for (int i = 0; i < B; ++i) {
-                const int64_t d = r * B + i;
-                const T out = fixed[d] ? T(0) : acc[i];
-                y[d] = out;
-                T pd = x[d];
-                if (FUSE) {
-                    pd = fma(beta, pd, z[d]);
-                    pout[d] = pd;
+                for (int i = 0; i < B; ++i) {
+                    const int64_t d = r * B + i;
+                    const T out = fixed[d] ? T(0) : acc[i];
+                    y[d] = out;
+                    T pd = x[d];
+                    if (FUSE) {
+                        pd = fma(beta, pd, z[d]);
+                        pout[d] = pd;
+                    }
+                    if (MODE == 1) dot += (double)(pd * out);
                 }
-                if (MODE == 1) dot += (double)(pd * out);
+            } else {
+                T res[B];
+#pragma unroll
+                for (int i = 0; i < B; ++i) res[i] = fixed[r * B + i] ? T(0) : bv[r * B + i] - acc[i];
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    T o = res[i];
+                    if constexpr (EPI == sfem_dev::SPMV_SMOOTH) {
+                        o = x[r * B + i];
+#pragma unroll
+                        for (int j = 0; j < B; ++j) o = fma(Mv[(r * B + i) * B + j], res[j], o);
+                        dot += (double)bv[r * B + i] * (double)o;
+                    }
+                    y[r * B + i] = o;
+                }
             }
+        }
+    }
+    if (MODE == 3) {
+        double tot, dummy;
+        if (reduce2_last(dot, 0.0, partial, &S->ticket[0], &tot, &dummy) && threadIdx.x == 0) {
+            S->rz_prev = S->rz;
+            S->rz = tot;
+            S->beta = S->rz_prev != 0.0 ? tot / S->rz_prev : 0.0;
         }
     }
     if (MODE == 1) {
@@ -278,7 +308,9 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
 // its nodal inverse, and keeps them in registers -- no shared-memory staging,
 // no barrier, B + B*B loads in flight per thread.  A warp's loads still cover
 // contiguous segments (32 consecutive nodes).
-template <typename T, int B, int PC, bool MIXED>
+// MGPRE (multigrid): z and minv are the fine level's pre-smoothing sweep and
+// smoother; r.z and beta are left to the cycle's last product.
+template <typename T, int B, int PC, bool MIXED, bool MGPRE = false>
 __global__ void __launch_bounds__(UPD_T)
 k_update_node(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
               const T *__restrict__ q, const T *__restrict__ minv, CgScalars *S, double *partial) {
@@ -329,9 +361,11 @@ k_update_node(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ 
     if (reduce2_last(rz, rr, partial, &S->ticket[1], &trz, &trr) && threadIdx.x == 0) {
         S->rr = trr;
         S->it += 1;
-        S->rz_prev = S->rz;
-        S->rz = trz;
-        S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        if (!MGPRE) {
+            S->rz_prev = S->rz;
+            S->rz = trz;
+            S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        }
         if (!(trr == trr)) {
             S->done = 1;
             S->status = SFEM_SINGULAR;
@@ -517,7 +551,7 @@ __global__ void k_fold(int64_t n, double *__restrict__ x64, float *__restrict__ 
 }
 
 // r64 = b - Kx64 (masked), r32 = (float) r64, z32 = M^-1 r32; reduce r.z, r.r.
-template <int B, int PC>
+template <int B, int PC, bool MGPRE = false>
 __global__ void __launch_bounds__(UPD_T)
 k_refresh(int64_t nN, const double *__restrict__ bvec, const double *__restrict__ Kx, const unsigned char *__restrict__ fixed,
           double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ z32, const float *__restrict__ minv,
@@ -554,8 +588,10 @@ k_refresh(int64_t nN, const double *__restrict__ bvec, const double *__restrict_
     if (reduce2_last(rz, rr, partial, &S->ticket[2], &trz, &trr) && threadIdx.x == 0) {
         S->rr = trr;
         S->rr_ref = trr;
-        S->rz = trz;
-        S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        if (!MGPRE) {
+            S->rz = trz;
+            S->beta = S->rz_prev != 0.0 ? trz / S->rz_prev : 0.0;
+        }
         S->refresh = 0;
         S->nrefresh += 1;
         if (trr <= S->tol2) {
@@ -583,7 +619,9 @@ k_true_residual(int64_t nd, const double *__restrict__ bvec, const double *__res
 }
 
 // initial z = M^-1 r and rz, rr (FP64 or FP32 vectors)
-template <typename T, int B, int PC>
+// MGPRE: z and minv are the multigrid's pre-smoothing sweep and smoother;
+// r.z is left at zero for the cycle's last product to set.
+template <typename T, int B, int PC, bool MGPRE = false>
 __global__ void __launch_bounds__(UPD_T)
 k_init(int64_t nN, const T *__restrict__ r, T *__restrict__ z, T *__restrict__ p, const T *__restrict__ minv,
        CgScalars *S, double *partial) {
@@ -609,6 +647,7 @@ k_init(int64_t nN, const T *__restrict__ r, T *__restrict__ z, T *__restrict__ p
     }
     double trz, trr;
     if (reduce2_last(rz, rr, partial, &S->ticket[3], &trz, &trr) && threadIdx.x == 0) {
+        if (MGPRE) trz = 0.0;
         S->rz = trz;
         S->rz_prev = trz;
         S->rr = trr;
@@ -616,6 +655,74 @@ k_init(int64_t nN, const T *__restrict__ r, T *__restrict__ z, T *__restrict__ p
         S->beta = 0.0;
     }
 }
+
+// ---- multigrid (sfem_mg.cuh) on the whole GPU: one launch per pass ----------
+
+// Structured-grid check of a mesh (0-based node ids, element index fastest):
+// *ok is cleared when an element differs from the meshgrid connectivity.
+__global__ void k_grid_check(const int *__restrict__ ien, int64_t nEl, int nen, int ndim, int ne, int *ok) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nEl) return;
+    for (int c = 0; c < nen; ++c)
+        if ((int64_t)ien[(int64_t)c * nEl + e] != mg_grid_node(ndim, ne, e, c) - 1) *ok = 0;
+}
+
+#define SFEM_GRID_LOOP                                                                 \
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;                 \
+    const int64_t gs = (int64_t)gridDim.x * blockDim.x;
+
+template <int NDIM, int B>
+__global__ void k_mg_fine(const sfem_dev::BatchArgs a, const BatchMesh M, const MgLevel F, const float *bj) {
+    SFEM_GRID_LOOP
+    sfem_dev::mg_pass_fine<NDIM, B>(a, M, F, bj, gt, gs);
+}
+template <int NDIM, int B>
+__global__ void k_mg_free(const sfem_dev::BatchArgs a, const BatchMesh M, const MgLevel F, const MgLevel C, int l) {
+    SFEM_GRID_LOOP
+    sfem_dev::mg_pass_free<NDIM, B>(a, M, F, C, l, gt, gs);
+}
+template <int NDIM, int B>
+__global__ void k_mg_galerkin(const sfem_dev::BatchArgs a, const BatchMesh M, const MgLevel F, const MgLevel C, int l,
+                              int *flag) {
+    SFEM_GRID_LOOP
+    sfem_dev::mg_pass_galerkin<NDIM, B>(a, M, F, C, l, gt, gs, flag);
+}
+template <int NDIM, int B>
+__global__ void k_mg_smoother(const MgLevel C, int *flag) {
+    SFEM_GRID_LOOP
+    sfem_dev::mg_pass_smoother<NDIM, B>(C, gt, gs, flag);
+}
+template <int NDIM, int B>
+__global__ void k_mg_coarsest(const MgLevel C, int n, float *cinv, double *gj, int *flag) {  // one CTA
+    sfem_dev::mg_pass_coarsest<NDIM, B>(C, n, cinv, gj, flag);
+}
+// cycle passes: each exits at once when the solve is done
+template <int NDIM, int B>
+__global__ void k_mg_restrict(const BatchMesh M, const MgLevel F, const MgLevel C, int l, int smooth,
+                              const CgScalars *S) {
+    if (S->done) return;
+    SFEM_GRID_LOOP
+    sfem_dev::mg_restrict<NDIM, B>(M, F, C, l, smooth != 0, gt, gs);
+}
+template <int NDIM, int B, int EPI>
+__global__ void k_mg_stencil(const MgLevel C, float *out, const CgScalars *S) {
+    if (S->done) return;
+    SFEM_GRID_LOOP
+    sfem_dev::mg_stencil_pass<NDIM, B, EPI>(C, out, gt, gs);
+}
+template <int NDIM, int B>
+__global__ void k_mg_prolong(const sfem_dev::BatchArgs a, const BatchMesh M, const MgLevel F, const MgLevel C, int l,
+                             const float *xc, const CgScalars *S) {
+    if (S->done) return;
+    SFEM_GRID_LOOP
+    sfem_dev::mg_prolong<NDIM, B>(a, M, F, C, l, xc, gt, gs);
+}
+__global__ void k_mg_csolve(const MgLevel C, int n, const float *cinv, const CgScalars *S) {
+    if (S->done) return;
+    SFEM_GRID_LOOP
+    sfem_dev::mg_coarse_solve(C, n, cinv, gt, gs);
+}
+#undef SFEM_GRID_LOOP
 
 // ---------------------------------------------------------------------------
 // host driver
@@ -667,6 +774,21 @@ class Solver {
     template <typename T, int B>
     void launch_spmv(const T *val, const T *x, T *y, bool fused);
     int read_scalars(CgScalars *h);
+    // multigrid (mixed precision, structured meshes)
+    int mg_detect();
+    template <int NDIM, int B>
+    int mg_build(const float *bj);
+    template <int NDIM, int B>
+    int mg_cycle(const float *r, float *z);
+    template <int B>
+    int mg_cycle_b(const float *r, float *z) {
+        if (m->ndim == 2) {
+            if constexpr (B <= 2) return mg_cycle<2, B>(r, z);
+        } else {
+            if constexpr (B != 2) return mg_cycle<3, B>(r, z);
+        }
+        return SFEM_UNSUPPORTED;
+    }
 
     sfem_ctx *ctx;
     sfem_matrix *K;
@@ -687,7 +809,117 @@ class Solver {
     int iterations = 0;
     int status = SFEM_OK;
     double relres = 0.0;
+    bool use_mg = false;
+    MgMesh mg{};
+    sfem_dev::BatchArgs mga{};  // the fields the hierarchy passes read: pattern, FP64 K, mask
+    BatchMesh mgM{};
+    int mg_launches = 0;        // kernels per cycle
 };
+
+// Elements per direction when the matrix's mesh is the structured meshgrid
+// grid (checked on the device once per mesh), else 0.
+int Solver::mg_detect() {
+    if (m->mg_ne >= 0) return m->mg_ne;
+    int ne = (m->fclass == SFEM_Q1 && m->nen == (1 << m->ndim)) ? mg_grid_ne(m->ndim, m->nN, m->nEl) : 0;
+    if (mg_levels(ne) < 2) ne = 0;
+    if (ne > 0) {
+        int *ok = nullptr, one = 1;
+        SFEM_TRY(alloc(&ok, 1, "grid check"));
+        SFEM_TRY(sfem_copy_in(ctx, ok, &one, sizeof(int), SFEM_MEM_HOST));
+        k_grid_check<<<(unsigned)sfem_cdiv(m->nEl, 256), 256, 0, ctx->stream>>>(m->ien, m->nEl, m->nen, m->ndim, ne, ok);
+        SFEM_LAUNCHED(ctx);
+        SFEM_TRY(sfem_copy_out(ctx, &one, ok, sizeof(int), SFEM_MEM_HOST));
+        if (!one) ne = 0;
+    }
+    m->mg_ne = ne;
+    return ne;
+}
+
+// The hierarchy of this solve's K: layout, fine smoother, Galerkin levels,
+// coarsest inverse.  bj: the FP32 block-Jacobi inverse.
+template <int NDIM, int B>
+int Solver::mg_build(const float *bj) {
+    const int ne = m->mg_ne;
+    const int64_t bytes = mg_layout(NDIM, B, ne, nd, nullptr, nullptr);
+    char *buf = nullptr;
+    SFEM_TRY(alloc(&buf, bytes, "multigrid"));
+    mg_layout(NDIM, B, ne, nd, buf, &mg);
+    memset(&mga, 0, sizeof(mga));
+    mga.sliceptr = m->sliceptr;
+    mga.col = m->col;
+    mga.rowlen = m->rowlen;
+    mga.val64 = K->val;
+    mga.fixed = fixed;
+    memset(&mgM, 0, sizeof(mgM));
+    mgM.nnode = m->nN;
+    mgM.slice1 = m->nslices;
+    int *flag = nullptr, zero = 0;
+    SFEM_TRY(alloc(&flag, 1, "multigrid status"));
+    SFEM_TRY(sfem_copy_in(ctx, flag, &zero, sizeof(int), SFEM_MEM_HOST));
+    auto grid = [&](int64_t work) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(sfem_cdiv(work, 256), 64 * ctx->num_sms)); };
+    const int L = mg.nlev, S = NDIM == 2 ? 9 : 27;
+    k_mg_fine<NDIM, B><<<grid(mg.lev[0].nnode), 256, 0, ctx->stream>>>(mga, mgM, mg.lev[0], bj);
+    for (int l = 0; l + 1 < L; ++l) {
+        k_mg_free<NDIM, B><<<grid(mg.lev[l + 1].nnode), 256, 0, ctx->stream>>>(mga, mgM, mg.lev[l], mg.lev[l + 1], l);
+        k_mg_galerkin<NDIM, B><<<grid((int64_t)mg.lev[l + 1].nnode * S), 256, 0, ctx->stream>>>(
+            mga, mgM, mg.lev[l], mg.lev[l + 1], l, flag);
+        ctx->launches += 2;
+        if (l + 2 < L) {
+            k_mg_smoother<NDIM, B><<<grid(mg.lev[l + 1].nnode), 256, 0, ctx->stream>>>(mg.lev[l + 1], flag);
+            SFEM_LAUNCHED(ctx);
+        }
+    }
+    k_mg_coarsest<NDIM, B><<<1, 512, 0, ctx->stream>>>(mg.lev[L - 1], mg.ndc, mg.cinv, mg.gj, flag);
+    SFEM_LAUNCHED(ctx);
+    SFEM_LAUNCHED(ctx);
+    int f = 0;
+    SFEM_TRY(sfem_copy_out(ctx, &f, flag, sizeof(int), SFEM_MEM_HOST));
+    if (f != 0) return sfem_set_error(ctx, f, "multigrid set-up failed (%d)", f);
+    return SFEM_OK;
+}
+
+// z = V(r) with the fine level's pre-smoothing sweep already in lev[0].x;
+// the last product reduces r.z and sets beta.  Every kernel exits at once
+// when the solve is done.
+template <int NDIM, int B>
+int Solver::mg_cycle(const float *r, float *z) {
+    using namespace sfem_dev;
+    const int L = mg.nlev;
+    auto grid = [&](int64_t work) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(sfem_cdiv(work, 256), 8 * ctx->num_sms)); };
+    const MgLevel &F0 = mg.lev[0];
+    int n = 0;
+    k_spmv_sym<float, B, 0, false, SPMV_RES><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+        K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, F0.x, F0.t, fixed, S, partial, nullptr,
+        nullptr, r, nullptr);
+    ++n;
+    for (int l = 1; l < L; ++l) {
+        k_mg_restrict<NDIM, B><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mgM, mg.lev[l - 1], mg.lev[l], l - 1,
+                                                                               l + 1 < L ? 1 : 0, S);
+        ++n;
+        if (l + 1 < L) {
+            k_mg_stencil<NDIM, B, SPMV_RES><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mg.lev[l], mg.lev[l].t, S);
+            ++n;
+        }
+    }
+    k_mg_csolve<<<1, 256, 0, ctx->stream>>>(mg.lev[L - 1], mg.ndc, mg.cinv, S);
+    ++n;
+    const float *xin = mg.lev[L - 1].x;
+    for (int l = L - 2; l >= 1; --l) {
+        k_mg_prolong<NDIM, B><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mga, mgM, mg.lev[l], mg.lev[l + 1], l,
+                                                                              xin, S);
+        k_mg_stencil<NDIM, B, SPMV_SMOOTH><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mg.lev[l], mg.lev[l].t, S);
+        n += 2;
+        xin = mg.lev[l].t;
+    }
+    k_mg_prolong<NDIM, B><<<grid(F0.nnode), 256, 0, ctx->stream>>>(mga, mgM, F0, mg.lev[1], 0, xin, S);
+    k_spmv_sym<float, B, 3, false, SPMV_SMOOTH><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+        K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, F0.x, z, fixed, S, partial, nullptr,
+        nullptr, r, F0.minv);
+    n += 2;
+    ctx->launches += n;
+    mg_launches = n;
+    return sfem_cuda_status(ctx, cudaGetLastError(), "multigrid cycle launch");
+}
 
 template <typename T, int B>
 void Solver::launch_spmv(const T *val, const T *x, T *y, bool fused) {
@@ -697,12 +929,12 @@ void Solver::launch_spmv(const T *val, const T *x, T *y, bool fused) {
                 auto kern = k_spmv_sym<float, B, 1>;
                 kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
                     K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial,
-                    nullptr, nullptr);
+                    nullptr, nullptr, nullptr, nullptr);
             } else {
                 auto kern = k_spmv_sym<float, B, 0>;
                 kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
                     K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial,
-                    nullptr, nullptr);
+                    nullptr, nullptr, nullptr, nullptr);
             }
             SFEM_LAUNCHED(ctx);
             return;
@@ -752,7 +984,8 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
                 if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
                 auto kern = k_spmv_sym<float, B, 1, true>;
                 kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN,
-                                                             m->nslices, pin, v.q, fixed, S, partial, v.z, pout);
+                                                             m->nslices, pin, v.q, fixed, S, partial, v.z, pout,
+                                                             nullptr, nullptr);
                 SFEM_LAUNCHED(ctx);
                 if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
                 pcur = pout;
@@ -766,7 +999,16 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
             launch_spmv<T, B>(val, v.p, v.q, true);
             if (profile) cudaEventRecord(events[2 * slot + 1], ctx->stream);
         }
-        {
+        bool mg_now = false;
+        if constexpr (MIXED) {
+            if (use_mg) {  // x, r and the multigrid's pre-smoothing sweep; r.z comes from the cycle
+                mg_now = true;
+                auto kern = k_update_node<T, B, PC, MIXED, true>;
+                kern<<<resident_grid(ctx, kern, UPD_T, upd_grid), UPD_T, 0, ctx->stream>>>(
+                    m->nN, v.x, v.r, mg.lev[0].x, pcur, v.q, mg.lev[0].minv, S, partial);
+            }
+        }
+        if (!mg_now) {
             auto kern = k_update_node<T, B, PC, MIXED>;
             kern<<<resident_grid(ctx, kern, UPD_T, upd_grid), UPD_T, 0, ctx->stream>>>(
                 m->nN, v.x, v.r, v.z, pcur, v.q, v.minv, S, partial);
@@ -779,12 +1021,17 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
             k_fold<<<std::min(vec_grid, small), 256, 0, ctx->stream>>>(nd, x64, (float *)v.x, S);
             k_spmv<double, B, 2><<<std::min(spmv_grid, small), SPMV_T, 0, ctx->stream>>>(
                 m->sliceptr, m->col, K->val, m->nN, m->nslices, x64, q64, fixed, S, partial);
-            k_refresh<B, PC><<<std::min(upd_grid, small), UPD_T, 0, ctx->stream>>>(
-                m->nN, bvec, q64, fixed, r64, (float *)v.r, (float *)v.z, (const float *)v.minv, S, partial);
+            if (mg_now)
+                k_refresh<B, PC, true><<<std::min(upd_grid, small), UPD_T, 0, ctx->stream>>>(
+                    m->nN, bvec, q64, fixed, r64, (float *)v.r, mg.lev[0].x, mg.lev[0].minv, S, partial);
+            else
+                k_refresh<B, PC><<<std::min(upd_grid, small), UPD_T, 0, ctx->stream>>>(
+                    m->nN, bvec, q64, fixed, r64, (float *)v.r, (float *)v.z, (const float *)v.minv, S, partial);
             ctx->launches += 3;
+            if (mg_now) (void)mg_cycle_b<B>((const float *)v.r, (float *)v.z);
         }
     };
-    const int per_iter = (MIXED ? 6 : 3) - (fuse_p ? 1 : 0);
+    const int per_iter = (MIXED ? 6 : 3) - (fuse_p ? 1 : 0) + (use_mg ? mg_launches : 0);
     if (profile) {
         events.resize(2 * chunk);
         for (auto &e : events) SFEM_CUDA(ctx, cudaEventCreate(&e));
@@ -841,7 +1088,7 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
 template <int B>
 int Solver::solve_b(double *x64) {
     const bool mixed = opts.precision == SFEM_MIXED;
-    const bool block = opts.precond == SFEM_PC_BLOCK_JACOBI && B > 1;
+    const bool block = opts.precond != SFEM_PC_JACOBI && B > 1;  // multigrid smooths with the block inverse
     const int mwidth = block ? B * B : B;
     // FP64 preconditioner inverse is built first, then cast for the FP32 path
     double *minv64 = nullptr;
@@ -895,11 +1142,39 @@ int Solver::solve_b(double *x64) {
         k_cast<float><<<vec_grid, 256, 0, ctx->stream>>>(nd, r0vec, v.r);
         SFEM_LAUNCHED(ctx);
         SFEM_LAUNCHED(ctx);
-        if (block)
-            k_init<float, B, 1><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
-        else
-            k_init<float, B, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
-        SFEM_LAUNCHED(ctx);
+        // multigrid: structured meshes with the upper-triangle FP32 K (else block Jacobi)
+        use_mg = false;
+        if (opts.precond == SFEM_PC_MULTIGRID && K->sym_state == 1 && opts.fp32_storage == SFEM_FP32_UPPER &&
+            mg_detect() > 0) {
+            if (m->ndim == 2) {
+                if constexpr (B <= 2) {
+                    SFEM_TRY((mg_build<2, B>(v.minv)));
+                    use_mg = true;
+                }
+            } else {
+                if constexpr (B != 2) {
+                    SFEM_TRY((mg_build<3, B>(v.minv)));
+                    use_mg = true;
+                }
+            }
+        }
+        if (use_mg) {
+            // first direction: z = V(r), with the pre-smoothing sweep from k_init
+            if (block)
+                k_init<float, B, 1, true><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, mg.lev[0].x, v.p,
+                                                                              mg.lev[0].minv, S, partial);
+            else
+                k_init<float, B, 0, true><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, mg.lev[0].x, v.p,
+                                                                              mg.lev[0].minv, S, partial);
+            SFEM_LAUNCHED(ctx);
+            SFEM_TRY(mg_cycle_b<B>(v.r, v.z));
+        } else {
+            if (block)
+                k_init<float, B, 1><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
+            else
+                k_init<float, B, 0><<<upd_grid, UPD_T, 0, ctx->stream>>>(m->nN, v.r, v.z, v.p, v.minv, S, partial);
+            SFEM_LAUNCHED(ctx);
+        }
         SFEM_TRY(block ? cg_loop<float, B, 1, true>(v, x64, r64, q64) : cg_loop<float, B, 0, true>(v, x64, r64, q64));
     }
     return SFEM_OK;
@@ -1083,7 +1358,7 @@ extern "C" int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t
     sfem_solve_opts_default(&o);
     if (opts) o = *opts;
     if (!(o.rtol >= 0.0) || o.maxit < 0 || (o.precision != SFEM_FP64 && o.precision != SFEM_MIXED) ||
-        (o.precond != SFEM_PC_JACOBI && o.precond != SFEM_PC_BLOCK_JACOBI) || !(o.reliable_delta > 0.0) ||
+        o.precond < SFEM_PC_JACOBI || o.precond > SFEM_PC_MULTIGRID || !(o.reliable_delta > 0.0) ||
         (o.fp32_storage != SFEM_FP32_UPPER && o.fp32_storage != SFEM_FP32_FULL) ||
         !(o.reliable_delta < 1.0))
         return sfem_set_error(ctx, SFEM_BAD_ARG, "bad solve options");
