@@ -182,12 +182,16 @@ k_gather(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, cons
     const int64_t slab0 = sliceptr[s], width = sliceptr[s + 1] - slab0;
     const int len = live ? rowlen[r] : 0;
     const int64_t q0 = live ? n2e_ptr[r] : 0, q1 = live ? n2e_ptr[r + 1] : 0;
+    GatherRow<NEN> R;
+    R.load(n2e, q0, q1, ien, nEl, r);
     for (int64_t k = 0; k < width; ++k) {
         const int64_t slab = slab0 + k;
         double acc[B * B];
 #pragma unroll
         for (int i = 0; i < B * B; ++i) acc[i] = 0.0;
-        if (k < len) {
+        if (k < len && R.fast) {
+            R.template add<B>(col[slab * 32 + lane], kbuf, nEl, acc);
+        } else if (k < len) {
             const int c = col[slab * 32 + lane];
             int prev = -1;
             for (int64_t q = q0; q < q1; ++q) {

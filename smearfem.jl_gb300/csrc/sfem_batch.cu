@@ -63,11 +63,11 @@ namespace {
 
 using namespace sfem_dev;
 
-// 2D classes fit two 512-thread CTAs per SM (64 registers); 3D elasticity and
-// the multigrid variants (whose hierarchy calls would spill at 64) take the
-// full register file of one.
+// 2D classes fit two 512-thread CTAs per SM (64 registers; the multigrid
+// variants spill some around the hierarchy's calls, and still run faster
+// than at one CTA per SM); 3D elasticity needs the full register file of one.
 template <int NDIM, int NEN, int NGP, int B, bool MIXED, bool MG>
-__global__ void __launch_bounds__(512, ((NDIM == 2 && !MG) ? 2 : 1)) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
+__global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid_constant__ ElemTableB tab, const __grid_constant__ BatchArgs a) {
     __shared__ double red[128];  // two halves, alternating (block_sum2)
     __shared__ double xch[4];
     __shared__ int s_flag, s_mesh;

@@ -187,3 +187,62 @@ __device__ __forceinline__ void load_v32(const float *__restrict__ v, int64_t sl
         out[8] = sfem_ld(b + 256 + lane, STREAM);
     }
 }
+
+// One row's share of the assembly gather (k_gather).  The row's elements, their
+// nodes and the row node's local position are read once, so each of the
+// row's slots costs one compare per element node instead of re-reading and
+// re-matching every element.  `fast` is false when the row lies in more than
+// MAXE elements or one of them repeats a node; callers then take their
+// general loop.  Blocks are added in ascending element order, the same order
+// (and so the same sums) as that general loop.
+template <int NEN>
+struct GatherRow {
+    static constexpr int MAXE = NEN == 9 ? 4 : NEN;  // elements around a node of a conforming Q1 / Q2 grid
+    int n;
+    bool fast;
+    int e[MAXE], a[MAXE], nodes[MAXE][NEN];
+
+    __device__ __forceinline__ void load(const int *__restrict__ n2e, int64_t q0, int64_t q1,
+                                         const int *__restrict__ ien, int64_t nEl, int r) {
+        n = (int)(q1 - q0);
+        fast = n <= MAXE;
+#pragma unroll
+        for (int m = 0; m < MAXE; ++m) {
+            const bool use = fast && m < n;
+            e[m] = use ? n2e[q0 + m] : 0;
+            a[m] = -1;
+#pragma unroll
+            for (int b = 0; b < NEN; ++b) {
+                nodes[m][b] = use ? __ldg(&ien[(int64_t)b * nEl + e[m]]) : -1;
+                if (nodes[m][b] == r) a[m] = b;
+            }
+            bool distinct = true;
+#pragma unroll
+            for (int b = 0; b < NEN; ++b)
+#pragma unroll
+                for (int c = b + 1; c < NEN; ++c) distinct = distinct && nodes[m][b] != nodes[m][c];
+            if (use && (a[m] < 0 || !distinct)) fast = false;
+        }
+    }
+
+    // acc += the element blocks of slot (row, c); kbuf: [pair][B][B][nEl]
+    template <int B>
+    __device__ __forceinline__ void add(int c, const double *__restrict__ kbuf, int64_t nEl, double *acc) const {
+#pragma unroll
+        for (int m = 0; m < MAXE; ++m) {
+            int hit = -1;
+#pragma unroll
+            for (int bq = 0; bq < NEN; ++bq) hit = nodes[m][bq] == c ? bq : hit;
+            if (m < n && hit >= 0) {
+                const int am = a[m];
+                const bool up = am <= hit;
+                const int64_t base = (int64_t)sfem_pair(up ? am : hit, up ? hit : am, NEN) * B * B;
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j)
+                        acc[i * B + j] += __ldg(&kbuf[(base + (up ? i * B + j : j * B + i)) * nEl + e[m]]);
+            }
+        }
+    }
+};

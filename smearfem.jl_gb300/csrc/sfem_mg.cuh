@@ -173,6 +173,19 @@ __device__ __forceinline__ int mg_stencil(const int ci[3], const int cj[3]) {
     return NDIM == 3 ? (cj[2] - ci[2] + 1) * 9 + s : s;
 }
 
+// Block (slab, lane) of the fine K in FP32: the lane-contiguous FP32 copy of
+// the batch and serving pipeline (one vector load), else the FP64 sliced-ELL
+// values rounded.
+template <int B>
+__device__ __forceinline__ void mg_fine_block(const BatchArgs &a, int64_t slab, int lane, float *blk) {
+    if (a.val32) {
+        load_v32<B, false>(a.val32, slab, lane, blk);
+    } else {
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) blk[e] = (float)a.val64[(slab * B * B + e) * 32 + lane];
+    }
+}
+
 // Free flags of the DOFs of node ci on level l.
 template <int NDIM, int B>
 __device__ __forceinline__ void mg_free(const BatchArgs &a, const BatchMesh &M, const MgLevel &L, int l,
@@ -202,8 +215,7 @@ __device__ __forceinline__ bool mg_block(const BatchArgs &a, const BatchMesh &M,
         const int lane = (int)(r & 31);
         const int64_t slab = a.sliceptr[r >> 5] + pos;
         if (pos >= a.rowlen[r] || a.col[slab * 32 + lane] != (int)(M.node0 + mg_index<NDIM>(cj, L.n))) return false;
-#pragma unroll
-        for (int e = 0; e < B * B; ++e) blk[e] = (float)a.val64[(slab * B * B + e) * 32 + lane];
+        mg_fine_block<B>(a, slab, lane, blk);
     } else {
         const int s = mg_stencil<NDIM>(ci, cj);
 #pragma unroll
@@ -278,8 +290,7 @@ __device__ __forceinline__ void mg_pass_fine(const BatchArgs &a, const BatchMesh
             const int64_t slab = slab0 + k;
             const int c = a.col[slab * 32 + lane];
             float blk[B * B];
-#pragma unroll
-            for (int e = 0; e < B * B; ++e) blk[e] = (float)a.val64[(slab * B * B + e) * 32 + lane];
+            mg_fine_block<B>(a, slab, lane, blk);
 #pragma unroll
             for (int i = 0; i < B; ++i)
 #pragma unroll
