@@ -205,6 +205,18 @@ def probe_fp64_peak(device):
 # CPU baseline: the C restatement of the reference, bounded sample
 # ---------------------------------------------------------------------------
 
+def _pcg_iteration_s(K, q, iters, threads):
+    """Seconds per Jacobi-PCG iteration of the oracle on K: the difference of
+    a 1-iteration and an (iters + 1)-iteration solve, after a warm-up solve
+    (the first solve also pays for first-touch of its work arrays)."""
+    K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=1, nthreads=threads)
+    _, st1 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=1, nthreads=threads)
+    _, st2 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=iters + 1, nthreads=threads)
+    if st2["iters"] != iters + 1 or not st2["seconds"] > st1["seconds"]:
+        raise RuntimeError(f"CPU PCG timing failed: {st1} {st2}")
+    return (st2["seconds"] - st1["seconds"]) / iters
+
+
 def cpu_sample(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=64, sample_iters=40):
     """Time the oracle's assembly of the ``sample_ne``^3 instance of the same
     generator (element loop + COO->CSC, scaled by the element-count ratio)
@@ -218,9 +230,7 @@ def cpu_sample(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=64, sam
     t0 = time.perf_counter()
     K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3, nthreads=threads)
     t_asm = time.perf_counter() - t0
-    _, st1 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=1, nthreads=threads)
-    _, st2 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=sample_iters + 1, nthreads=threads)
-    t_iter = max(1e-9, (st2["seconds"] - st1["seconds"]) / sample_iters)
+    t_iter = _pcg_iteration_s(K, q, sample_iters, threads)
     _, _, nzs, _, n_s = K.arrays()
     nnz_s = len(nzs)
     del K
@@ -233,6 +243,54 @@ def cpu_sample(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=64, sam
                    f"generator scaled x{scale_el:.0f} by element count, plus {sample_iters} of its "
                    f"Jacobi-PCG iterations scaled by nnz ({nnz_full}/{nnz_s}) and by the "
                    f"{iters_full} iterations the full {ne_full}^3 solve takes")}
+
+
+def cpu_single_thread(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=32, sample_iters=20):
+    """The same estimate as cpu_sample with ONE thread (the reference's serial
+    element loop): the sample_ne^3 instance's assembly and sample_iters of
+    its Jacobi-PCG iterations, scaled to the full workload."""
+    from oracle import coracle
+    q = pkg.meshgen.jittered_cube(ne=sample_ne)
+    t0 = time.perf_counter()
+    K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3, nthreads=1)
+    t_asm = time.perf_counter() - t0
+    t_iter = _pcg_iteration_s(K, q, sample_iters, 1)
+    nnz_s = len(K.arrays()[2])
+    del K
+    scale_el = (ne_full / sample_ne) ** 3
+    t_full = t_asm * scale_el + t_iter * (nnz_full / nnz_s) * iters_full
+    return {"value": n_dof_full / t_full, "unit": UNIT, "cores": 1, "est_full_s": t_full,
+            "sample": (f"oracle on one thread: {sample_ne}^3 assembly scaled x{scale_el:.0f} by element count, "
+                       f"plus {sample_iters} Jacobi-PCG iterations scaled by nnz and by {iters_full} iterations")}
+
+
+def dense_inverse_solve(pkg, sample_ne=10):
+    """The reference's own solve (examples/vector3D.jl:318,320: the dense
+    inverse of K_free) on the 20^3 parity problem, estimated from the
+    sample_ne^3 instance with the same boundary conditions: NumPy's LAPACK
+    inverse timed there and scaled by (n_free(20^3) / n_free(sample))^3."""
+    import os
+    from oracle import coracle
+    q = pkg.meshgen.hex_problem(sample_ne, 1001, jitter=0.0, top="sin", rtol=1e-12)
+    full = pkg.meshgen.parity_cube20()
+    K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3,
+                         nthreads=coracle.max_threads())
+    colptr, rowval, nzval, _, n = K.arrays()
+    del K
+    import scipy.sparse as sp
+    Kc = sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(n, n))
+    free = np.setdiff1d(np.arange(n), q.fixed_dofs - 1)
+    Kff = Kc[free][:, free].toarray()
+    t0 = time.perf_counter()
+    np.linalg.inv(Kff)
+    t = time.perf_counter() - t0
+    nf_full = full.n_dof - len(full.fixed_dofs)
+    threads = os.environ.get("OPENBLAS_NUM_THREADS") or os.environ.get("OMP_NUM_THREADS") or str(os.cpu_count())
+    est = t * (nf_full / len(free)) ** 3
+    return {"problem": "20^3 parity cube (27,783 DOF, 26,019 free)", "est_s": est,
+            "dof_per_s": full.n_dof / est, "threads": int(threads),
+            "sample": f"numpy.linalg.inv of the {len(free)}-DOF K_free of the {sample_ne}^3 instance: "
+                      f"{t:.3f} s, scaled by (26019/{len(free)})^3"}
 
 
 def reference_arm(args, dist):
@@ -463,7 +521,9 @@ def our_arm(args, dist):
         # ---- CPU baseline (rank 0, N=1 only)
         v, det = cpu_sample(pkg, args.ne, n_dof, nnz, it)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",
-                                "sample": det["sample"]}
+                                "sample": det["sample"],
+                                "single_thread": cpu_single_thread(pkg, args.ne, n_dof, nnz, it),
+                                "reference_dense_solve": dense_inverse_solve(pkg)}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0
