@@ -314,6 +314,7 @@ int sfem_gather_blocks(sfem_ctx *ctx, const sfem_mesh *m, const double *kbuf, do
 
 extern "C" int sfem_assemble(sfem_ctx *ctx, sfem_mesh *m, int plane, const double *Young, int64_t nYoung,
                              const double *nu, int64_t nNu, int mem_space, sfem_matrix **out) {
+    SfemRange range_("sfem assemble");
     if (!ctx || !m || !out) return SFEM_BAD_ARG;
     *out = nullptr;
     cudaSetDevice(ctx->device);

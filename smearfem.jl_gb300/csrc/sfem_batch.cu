@@ -604,6 +604,7 @@ extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const 
                                 const double *nu, int64_t nNu, const int64_t *fix_offsets, const int64_t *fixed_dofs,
                                 const double *fixed_vals, double *u_out, int mem_space, const sfem_solve_opts *opts,
                                 sfem_batch_stats *stats) {
+    SfemRange range_("sfem batch solve");
     if (!ctx || !bt || !u_out || !fix_offsets) return SFEM_BAD_ARG;
     cudaSetDevice(ctx->device);
     sfem_solve_opts o;

@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <string>
 
 #include "smearfem_gpu.h"
@@ -111,6 +113,16 @@ int sfem_mesh_create_nel(sfem_ctx *ctx, int ndim, int function_class, int nDof, 
 #define SFEM_CUDA(ctx, expr) SFEM_TRY(sfem_cuda_status((ctx), (expr), #expr))
 
 #define SFEM_LAUNCHED(ctx) ((ctx)->launches++)
+
+// Scoped NVTX range around a library phase (pattern, assembly, Dirichlet
+// set-up, hierarchy, PCG, batch and serving work): visible to Nsight tools,
+// free when none is attached.
+struct SfemRange {
+    explicit SfemRange(const char *name) { nvtxRangePushA(name); }
+    ~SfemRange() { nvtxRangePop(); }
+    SfemRange(const SfemRange &) = delete;
+    SfemRange &operator=(const SfemRange &) = delete;
+};
 
 // ---- device helpers -------------------------------------------------------
 __device__ __forceinline__ void sfem_dev_error(DevErr *e, int code, long long index) {

@@ -362,6 +362,7 @@ extern "C" int sfem_mesh_destroy(sfem_mesh *m) {
 }
 
 extern "C" int sfem_pattern_build(sfem_ctx *ctx, sfem_mesh *m, int64_t *n_out, int64_t *nnz_out) {
+    SfemRange range_("sfem pattern");
     if (!ctx || !m) return SFEM_BAD_ARG;
     cudaSetDevice(ctx->device);
     if (m->has_pattern) {

@@ -422,6 +422,7 @@ void release_request_buffers(sfem_server *s, Request *r) {
 
 // Place one request on the device and publish it (worker thread, mutex not held).
 int place_request(sfem_server *s, Request *r) {
+    SfemRange range_("sfem serve place");
     sfem_ctx *ctx = s->ctx;
     const int b = r->b, nd_ = r->ndim;
     sfem_mesh *m = nullptr;

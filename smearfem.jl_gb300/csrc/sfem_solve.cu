@@ -839,6 +839,7 @@ int Solver::mg_detect() {
 // coarsest inverse.  bj: the FP32 block-Jacobi inverse.
 template <int NDIM, int B>
 int Solver::mg_build(const float *bj) {
+    SfemRange range_("sfem multigrid set-up");
     const int ne = m->mg_ne;
     const int64_t bytes = mg_layout(NDIM, B, ne, nd, nullptr, nullptr);
     char *buf = nullptr;
@@ -960,6 +961,7 @@ int Solver::read_scalars(CgScalars *h) {
 
 template <typename T, int B, int PC, bool MIXED>
 int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
+    SfemRange range_("sfem pcg");
     const T *val = nullptr;
     if constexpr (sizeof(T) == 8) val = (const T *)K->val;
     else val = (const T *)K->val32;
@@ -1351,6 +1353,7 @@ extern "C" void sfem_solve_opts_default(sfem_solve_opts *o) {
 extern "C" int sfem_solve_dirichlet(sfem_ctx *ctx, sfem_matrix *K, const int64_t *fixed_dofs, int64_t nfix,
                                     const double *fixed_vals, const double *f, double *u_out, int mem_space,
                                     const sfem_solve_opts *opts, sfem_solve_stats *stats) {
+    SfemRange range_("sfem solve");
     if (!ctx || !K || !u_out) return SFEM_BAD_ARG;
     if (nfix < 0 || (nfix > 0 && (!fixed_dofs || !fixed_vals))) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad fixed DOF list");
     cudaSetDevice(ctx->device);
