@@ -35,6 +35,10 @@ struct SolveOpts
     fp32_storage::Cint
 end
 
+# :jacobi, :block_jacobi, or :multigrid (mixed precision on meshgrid meshes; block Jacobi elsewhere)
+_precond(p::Symbol) = p === :jacobi ? Cint(0) : p === :block_jacobi ? Cint(1) : p === :multigrid ? Cint(2) :
+    throw(ArgumentError("precond must be :jacobi, :block_jacobi or :multigrid"))
+
 mutable struct SolveStats
     status::Cint
     iterations::Cint
@@ -165,7 +169,7 @@ function solve_dirichlet(K::GPUMatrix, fixed_dofs, fixed_vals, f=nothing; precis
     fd = Int64.(collect(fixed_dofs)); fv = Float64.(collect(fixed_vals))
     fp = f === nothing ? C_NULL : Float64.(collect(f))
     u = Vector{Float64}(undef, K.n)
-    opts = SolveOpts(precision == :mixed ? 1 : 0, precond == :block_jacobi ? 1 : 0, rtol, maxit, 32, 0.1, 0, 0)
+    opts = SolveOpts(precision == :mixed ? 1 : 0, _precond(precond), rtol, maxit, 32, 0.1, 0, 0)
     stats = SolveStats()
     GC.@preserve fd fv fp u begin
         st = ccall((:sfem_solve_dirichlet, libsfem), Cint,
@@ -212,7 +216,7 @@ function solve_increments(K::GPUMatrix, fixed_dofs, fixed_vals::AbstractMatrix; 
     fd = Int64.(collect(fixed_dofs)); fv = convert(Matrix{Float64}, fixed_vals)
     nsteps = size(fv, 2)
     U = Matrix{Float64}(undef, K.n, nsteps)
-    opts = SolveOpts(precision == :mixed ? 1 : 0, precond == :block_jacobi ? 1 : 0, rtol, maxit, 32, 0.1, 0, 0)
+    opts = SolveOpts(precision == :mixed ? 1 : 0, _precond(precond), rtol, maxit, 32, 0.1, 0, 0)
     GC.@preserve fd fv U begin
         st = ccall((:sfem_solve_increments, libsfem), Cint,
                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Int64, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Ptr{Cdouble},
