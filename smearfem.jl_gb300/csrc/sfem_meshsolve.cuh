@@ -109,6 +109,10 @@ struct BatchArgs {
     int64_t u_len;   // entries of u_out (zeroed by the serving kernel)
     const double *u_init;  // initial guess in u_out's numbering (a previous solution), or null
     const MgMesh *mg;      // per mesh: multigrid hierarchy (used when its nlev >= 2), or null
+    // upper-triangle FP32 copy of K (single-mesh solver), read by the hierarchy's Galerkin pass
+    const int64_t *sptrU;
+    const int *colU;
+    const float *valU;
     // solver
     double rtol, delta2;
     int maxit, block_jacobi;

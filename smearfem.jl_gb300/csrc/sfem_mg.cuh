@@ -195,15 +195,40 @@ __device__ __forceinline__ void mg_free(const BatchArgs &a, const BatchMesh &M, 
     for (int c = 0; c < B; ++c) f[c] = l == 0 ? a.fixed[(M.node0 + li) * B + c] == 0 : L.fr[li * B + c] != 0;
 }
 
-// Block A_l(i, j) of neighbours i, j on level l: the sliced-ELL K (FP64,
-// rounded to FP32) on the fine level (the position of j among i's ascending neighbours follows
+// Block A_l(i, j) of neighbours i, j on level l: on the fine level the
+// upper-triangle FP32 copy when there is one, else the sliced-ELL K (FP32
+// copy, or FP64 rounded) (the position of j among i's ascending neighbours follows
 // from the grid), the stencil on coarse levels.  False when the fine
 // pattern is not the structured one.
 template <int NDIM, int B>
 __device__ __forceinline__ bool mg_block(const BatchArgs &a, const BatchMesh &M, const MgLevel &L, int l,
                                          const int ci[3], const int cj[3], float *blk) {
     const int64_t li = mg_index<NDIM>(ci, L.n);
-    if (l == 0) {
+    if (l == 0 && a.valU) {  // upper-triangle FP32 copy: block (i, j) for j >= i, else (j, i) transposed
+        const int64_t gi = M.node0 + li, gj = M.node0 + mg_index<NDIM>(cj, L.n);
+        const bool up = gj >= gi;
+        const int *ro = up ? ci : cj, *co = up ? cj : ci;  // the owning row and the column, grid coordinates
+        int pos = 0, kd = 0, mul = 1;
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) {
+            const int lo = ro[d] > 0 ? 1 : 0;
+            pos += (co[d] - ro[d] + lo) * mul;
+            kd += lo * mul;  // the diagonal's position in the full row
+            mul *= 1 + lo + (ro[d] < L.n ? 1 : 0);
+        }
+        const int64_t r = up ? gi : gj, c = up ? gj : gi;
+        const int lane = (int)(r & 31);
+        const int64_t u0 = a.sptrU[r >> 5], ku = pos - kd;
+        if (ku < 0 || ku >= a.sptrU[(r >> 5) + 1] - u0) return false;
+        const int64_t slab = u0 + ku;
+        if (a.colU[slab * 32 + lane] != (int)c) return false;
+        float t[B * B];
+        load_v32<B, false>(a.valU, slab, lane, t);
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j) blk[i * B + j] = up ? t[i * B + j] : t[j * B + i];
+    } else if (l == 0) {
         int pos = 0, mul = 1;
 #pragma unroll
         for (int d = 0; d < NDIM; ++d) {

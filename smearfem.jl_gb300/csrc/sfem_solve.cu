@@ -851,6 +851,9 @@ int Solver::mg_build(const float *bj) {
     mga.rowlen = m->rowlen;
     mga.val64 = K->val;
     mga.fixed = fixed;
+    mga.sptrU = K->sptrU;  // the Galerkin pass reads the upper-triangle FP32 copy
+    mga.colU = K->colU;
+    mga.valU = K->valU;
     memset(&mgM, 0, sizeof(mgM));
     mgM.nnode = m->nN;
     mgM.slice1 = m->nslices;
