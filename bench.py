@@ -70,8 +70,8 @@ def parse_args(argv=None):
     ap.add_argument("--mixed-precond", default="both", choices=["both", "block_jacobi", "multigrid"],
                     help="preconditioners of the mixed leg (profiling runs pick one)")
     ap.add_argument("--mg-delta", type=float, default=0.01,
-                    help="reliable-update factor of the mixed multigrid solve (multigrid drops the FP32 "
-                         "residual 10x in 2-3 iterations; 0.01 halves the FP64 refreshes at the same error)")
+                    help="reliable-update factor of the multigrid solves (mixed, batch, serve): multigrid drops "
+                         "the FP32 residual 10x in 2-3 iterations; 0.01 halves the FP64 refreshes at the same error")
     ap.add_argument("--batch-precond", default="multigrid", choices=["multigrid", "block_jacobi"],
                     help="batch-leg preconditioner (multigrid: structured meshes)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
@@ -606,6 +606,7 @@ def batch_leg(args, pkg, ctx, stream, dist):
     # the workload states PCG to 1e-8; the metric needs 1e-8 error in u, which
     # this stiff plane-strain family reaches at a 1e-12 relative residual
     rtol = args.batch_rtol
+    delta = args.mg_delta if args.batch_precond == "multigrid" else 0.1
     t0 = time.perf_counter()
     # tuning trials: full solves of a quarter of the meshes, taken evenly
     # from the size order (capping iterations would hide what clusters buy on
@@ -615,12 +616,13 @@ def batch_leg(args, pkg, ctx, stream, dist):
         shape, tuned_ms = bt.launch(), None
     else:
         shape, tuned_ms = bt.autotune(1.0, nus, fixed, vals, plane="strain", precision="mixed",
-                                      precond=args.batch_precond, rtol=rtol, sample=max(1, len(probs) // 4))
+                                      precond=args.batch_precond, rtol=rtol, sample=max(1, len(probs) // 4),
+                                      reliable_delta=delta)
     t_tune = time.perf_counter() - t0
 
     def run_batch():
         return bt.solve(1.0, nus, fixed, vals, plane="strain", precision="mixed",
-                        precond=args.batch_precond, rtol=rtol)
+                        precond=args.batch_precond, rtol=rtol, reliable_delta=delta)
 
     for _ in range(args.warmup):
         u, st = run_batch()
@@ -782,6 +784,7 @@ def serve_leg(args, pkg, ctx, dist):
     # 8-CTA clusters of 256 threads (two per SM): measured 5% above 4 x 512 on this stream
     cl, th = (int(v) for v in args.serve_launch.split(","))
     srv = pkg.Server(precision="mixed", precond=args.serve_precond, rtol=rtol, cluster=cl, threads=th,
+                     reliable_delta=args.mg_delta if args.serve_precond == "multigrid" else 0.1,
                      sm_fraction=1.0, idle_exit_ms=200.0)
     try:
         # warm-up: every pool mesh once (builds and caches each topology's pattern)
