@@ -200,7 +200,8 @@ __device__ __forceinline__ void load_v32(const float *__restrict__ v, int64_t sl
     }
 }
 
-// One row's share of the assembly gather (k_gather).  The row's elements, their
+// One row's share of the assembly gather (k_gather, and the multigrid
+// instantiations of the per-mesh pipeline).  The row's elements, their
 // nodes and the row node's local position are read once, so each of the
 // row's slots costs one compare per element node instead of re-reading and
 // re-matching every element.  `fast` is false when the row lies in more than

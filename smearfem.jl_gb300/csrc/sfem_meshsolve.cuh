@@ -708,12 +708,19 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
             const int64_t slab0 = a.sliceptr[s], width = a.sliceptr[s + 1] - slab0;
             const int len = liver ? a.rowlen[r] : 0;
             const int64_t q0 = liver ? a.n2e_ptr[r] : 0, q1 = liver ? a.n2e_ptr[r + 1] : 0;
+            // the multigrid instantiations (calls of their own in the serving kernel) read each
+            // row's element lists once; the others keep the loop below and its register budget
+            GatherRow<NEN> R;
+            R.fast = false;
+            if constexpr (MGOK) R.load(a.n2e, q0, q1, a.ien, a.nEl, r);
             for (int64_t k = 0; k < width; ++k) {
                 const int64_t slab = slab0 + k;
                 double acc[B * B];
 #pragma unroll
                 for (int i = 0; i < B * B; ++i) acc[i] = 0.0;
-                if (k < len) {
+                if (MGOK && k < len && R.fast) {
+                    R.template add<B>(a.col[slab * 32 + lane], a.kbuf, a.nEl, acc);
+                } else if (k < len) {
                     const int c = a.col[slab * 32 + lane];
                     int prev = -1;
                     for (int64_t qq = q0; qq < q1; ++qq) {
