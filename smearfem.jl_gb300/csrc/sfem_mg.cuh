@@ -1,7 +1,8 @@
-// Geometric multigrid preconditioner for the per-mesh solver (process_mesh)
-// on structured Q1 meshes: the node numbering and connectivity of the
-// reference's meshgrid (examples/vector3D.jl:66-101), ne elements per
-// direction, x fastest.
+// Geometric multigrid preconditioner for structured Q1 meshes (the node
+// numbering and connectivity of the reference's meshgrid,
+// examples/vector3D.jl:66-101; ne elements per direction, x fastest), used by
+// the per-mesh pipeline of batches and servers (process_mesh, one group per
+// mesh) and, as grid-wide launches, by the single-mesh mixed solver.
 //
 // Hierarchy.  Level l has n_l elements per direction; n_{l+1} = ceil(n_l / 2)
 // until n <= 2.  Coarse node I sits on fine node c(I) = min(2I, n_l) in each
@@ -13,8 +14,8 @@
 // fine DOF is, so P' = diag(free_f) P diag(free_c).
 //
 // Coarse operators are Galerkin products A_{l+1} = P'^T A_l P' with A_0 the
-// masked K rounded to FP32.  Their node pattern is again the 3^ndim neighbourhood, so
-// they are stored as stencils: block (I, I + offset s) at
+// masked K rounded to FP32.  Their node pattern is again the 3^ndim
+// neighbourhood, so they are stored as stencils: block (I, I + offset s) at
 // A[(s * B*B + e) * nnode + I], zero where the neighbour is off the grid.
 //
 // Cycle: V(1,1) with l1-scaled block Jacobi (x += w_i D_i^-1 r_i with
@@ -25,8 +26,9 @@
 // is the same operator, so the cycle is a symmetric positive definite
 // preconditioner for CG.
 //
-// Everything is group-wide with plain group barriers between the passes and
-// no atomics on values: a mesh's result does not depend on what else runs.
+// Every pass is a loop over the group's (or the grid's) threads with a
+// barrier (or a launch boundary) after it, and no atomics on values: a
+// mesh's result does not depend on what else runs.
 //
 // Included by sfem_meshsolve.cuh after the group SpMV and the group types.
 #pragma once
@@ -195,11 +197,11 @@ __device__ __forceinline__ void mg_free(const BatchArgs &a, const BatchMesh &M, 
     for (int c = 0; c < B; ++c) f[c] = l == 0 ? a.fixed[(M.node0 + li) * B + c] == 0 : L.fr[li * B + c] != 0;
 }
 
-// Block A_l(i, j) of neighbours i, j on level l: on the fine level the
-// upper-triangle FP32 copy when there is one, else the sliced-ELL K (FP32
-// copy, or FP64 rounded) (the position of j among i's ascending neighbours follows
-// from the grid), the stencil on coarse levels.  False when the fine
-// pattern is not the structured one.
+// Block A_l(i, j) of neighbours i, j on level l.  Fine level: the
+// upper-triangle FP32 copy when there is one, else the sliced-ELL K (its
+// FP32 copy, or FP64 rounded); the position of j among i's ascending
+// neighbours follows from the grid.  Coarse levels: the stencil.  False
+// when the fine pattern is not the structured one.
 template <int NDIM, int B>
 __device__ __forceinline__ bool mg_block(const BatchArgs &a, const BatchMesh &M, const MgLevel &L, int l,
                                          const int ci[3], const int cj[3], float *blk) {
