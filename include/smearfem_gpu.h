@@ -193,7 +193,9 @@ typedef struct {
     int maxit;            /* iteration cap (SFEM_NOT_CONVERGED beyond it)          */
     int check_every;      /* iterations per device-side chunk between host checks */
     double reliable_delta;/* mixed: refresh the FP64 residual when the FP32
-                             residual has dropped by this factor                 */
+                             residual has dropped by this factor (0.1; with
+                             SFEM_PC_MULTIGRID, 0.01 refreshes half as often
+                             at the same error)                                 */
     int profile;          /* 1: time the SpMV launches with CUDA events           */
     int fp32_storage;     /* SFEM_MIXED: SFEM_FP32_UPPER (default) stores the
                              upper-triangle blocks of K once (K is symmetric);
