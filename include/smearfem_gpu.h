@@ -299,6 +299,19 @@ SFEM_API int sfem_batch_get_launch(const sfem_batch *batch, int *threads, int *c
                                    int *cluster, int64_t *cluster_min_nodes, int *last_grid);
 SFEM_API int sfem_batch_destroy(sfem_batch *batch);
 
+/* ---- multigrid: which meshes get a hierarchy -------------------------------- */
+
+/* Host-only query (no device, no context).  ne_out: elements per direction
+ * when the mesh is the structured grid the reference's meshgrid makes
+ * (examples/vector3D.jl:66-101: (ne+1)^ndim nodes, ne^ndim Q1 elements, its
+ * node numbering and connectivity), else 0.  levels_out / bytes_out: the
+ * SFEM_PC_MULTIGRID hierarchy of such a mesh (levels, the fine one included;
+ * device bytes on top of the CG's), 0 when it gets none (other meshes, Q2,
+ * ne < 3).  IEN: nEl x nen, column-major, 1-based, host memory. */
+SFEM_API int sfem_multigrid_info(int ndim, int function_class, int nDof, int64_t nNodes,
+                                 const int64_t *IEN, int64_t nEl, int *ne_out, int *levels_out,
+                                 int64_t *bytes_out);
+
 /* ---- on-device mesh generation --------------------------------------------- */
 
 /* The reference's structured grid generator (examples/vector3D.jl:10-130) on

@@ -8,5 +8,6 @@ reference's Julia calling surface plus the seeded mesh generators.
 from ._lib import SfemError, lib  # noqa: F401
 from .fem import (Batch, Context, Matrix, Mesh, Server, apply_boundary_conditions,  # noqa: F401
                   assemble_system, basis_function, gaussian_quadrature, get_context,
-                  inflate_sphere, meshgrid, solve_dirichlet, version, write_scene, write_vtk)
+                  inflate_sphere, meshgrid, multigrid_info, solve_dirichlet, version, write_scene,
+                  write_vtk)
 from . import meshgen  # noqa: F401

@@ -116,6 +116,8 @@ SIGNATURES = {
     "sfem_batch_get_launch": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), I64P, C.POINTER(C.c_int)]),
     "sfem_batch_destroy": (C.c_int, [P]),
+    "sfem_multigrid_info": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, I64P, C.c_int64,
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int), I64P]),
     "sfem_solve_dirichlet": (C.c_int, [P, P, P, I64, P, P, P, C.c_int, C.POINTER(SolveOpts),
                                        C.POINTER(SolveStats)]),
     "sfem_penalty_add": (C.c_int, [P, P, P, P, I64, C.c_int, C.c_double, C.c_int]),

@@ -705,6 +705,19 @@ extern "C" int sfem_batch_get_launch(const sfem_batch *bt, int *threads, int *ct
     return SFEM_OK;
 }
 
+extern "C" int sfem_multigrid_info(int ndim, int function_class, int nDof, int64_t nNodes, const int64_t *IEN,
+                                   int64_t nEl, int *ne_out, int *levels_out, int64_t *bytes_out) {
+    if (ndim != 2 && ndim != 3) return SFEM_BAD_ARG;
+    if ((nDof != 1 && nDof != ndim) || nNodes < 1 || nEl < 1 || !IEN) return SFEM_BAD_ARG;
+    const int nen = function_class == SFEM_Q2 ? 9 : (1 << ndim);
+    const int ne = mg_structured_ne(ndim, function_class, nen, nNodes, nEl, IEN, nEl);
+    const int L = mg_levels(ne);
+    if (ne_out) *ne_out = ne;
+    if (levels_out) *levels_out = L;
+    if (bytes_out) *bytes_out = L >= 2 ? mg_layout(ndim, nDof, ne, (nNodes + 31) / 32 * 32 * nDof, nullptr, nullptr) : 0;
+    return SFEM_OK;
+}
+
 extern "C" int sfem_batch_destroy(sfem_batch *bt) {
     if (!bt) return SFEM_OK;
     sfem_ctx *ctx = bt->ctx;

@@ -625,6 +625,20 @@ def assemble_system(ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1, ID=None
         K.close()
 
 
+def multigrid_info(nNodes, IEN, ndim, nDof=None, FunctionClass="Q1"):
+    """Whether ``precond="multigrid"`` gives this mesh a hierarchy (host only,
+    no GPU): ``{"ne": elements per direction of the meshgrid grid or 0,
+    "levels": hierarchy levels or 0, "bytes": its device memory}``.
+    ``IEN`` is the reference's nEl x nen array (1-based)."""
+    nDof = int(nDof if nDof is not None else ndim)
+    E = _Buf(IEN, np.int64)
+    nEl = int(np.shape(IEN)[0])
+    ne, lv, nb = C.c_int(), C.c_int(), C.c_int64()
+    check(lib().sfem_multigrid_info(int(ndim), {"Q1": L.Q1, "Q2": L.Q2}[FunctionClass], nDof, int(nNodes),
+                                    C.cast(E.ptr, L.I64P), nEl, C.byref(ne), C.byref(lv), C.byref(nb)))
+    return {"ne": ne.value, "levels": lv.value, "bytes": nb.value}
+
+
 def meshgrid(x0, x1, y0, y1, z0, z1, ne, ndim, device=False, ctx=None):
     """The reference's ``meshgrid`` (examples/vector3D.jl:10-130) generated on
     the GPU.  Returns ``(NodeList, IEN, ID, IEN_top, IEN_btm)`` in the

@@ -15,7 +15,8 @@ module smearFEMGPU
 using SparseArrays
 
 export assemble_system, gaussian_quadrature, basis_function, solve_dirichlet, GPUMatrix,
-       apply_boundary_conditions!, solve_increments, meshgrid, inflate_sphere, write_vtk, write_scene
+       apply_boundary_conditions!, solve_increments, meshgrid, inflate_sphere, write_vtk, write_scene,
+       multigrid_info
 
 const libsfem = get(ENV, "SMEARFEM_GPU_LIB", joinpath(@__DIR__, "..", "lib", "libsmearfem_gpu.so"))
 
@@ -226,6 +227,24 @@ function solve_increments(K::GPUMatrix, fixed_dofs, fixed_vals::AbstractMatrix; 
     end
     check(st, ctx)
     return U
+end
+
+"""
+    multigrid_info(nNodes, IEN, ndim; nDof=ndim, FunctionClass="Q1")
+
+Whether `precond=:multigrid` gives this mesh a hierarchy (host only, no GPU):
+`(ne, levels, bytes)` with `ne` the elements per direction of a meshgrid mesh
+(0 for any other mesh) and the hierarchy's levels and device bytes.
+"""
+function multigrid_info(nNodes, IEN::AbstractMatrix, ndim; nDof=ndim, FunctionClass="Q1")
+    I = Matrix{Int64}(IEN)
+    ne = Ref{Cint}(0); lv = Ref{Cint}(0); nb = Ref{Int64}(0)
+    fc = FunctionClass == "Q2" ? SFEM_Q2 : SFEM_Q1
+    st = GC.@preserve I ccall((:sfem_multigrid_info, libsfem), Cint,
+                              (Cint, Cint, Cint, Int64, Ptr{Int64}, Int64, Ref{Cint}, Ref{Cint}, Ref{Int64}),
+                              ndim, fc, nDof, nNodes, I, size(I, 1), ne, lv, nb)
+    st == SFEM_OK || throw(ErrorException("sfem_multigrid_info: status $st"))
+    return (ne = Int(ne[]), levels = Int(lv[]), bytes = nb[])
 end
 
 """
