@@ -333,7 +333,9 @@ def reference_arm(args, dist):
                    "iterations_full_estimate": iters_full,
                    "iterations_sample_full_solve": st["iters"]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": det["cores"], "kind": "port",
-                         "sample": det["sample"]},
+                         "sample": det["sample"],
+                         "single_thread": cpu_single_thread(pkg, ne, n_dof, nnz, iters_full),
+                         "reference_dense_solve": dense_inverse_solve(pkg)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
