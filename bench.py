@@ -10,15 +10,22 @@ mesh upload/validation, device sparsity pattern, FP64 element stiffness and
 assembly, Dirichlet elimination and Jacobi-PCG to 1e-10 relative residual.
 
   value     DOF / step time, inputs already resident in HBM (FP64 path)
-  mixed     the same step with the FP32-inner / FP64-refresh solver
+  mixed     the same step with the FP32-inner / FP64-refresh solver, with
+            block Jacobi and with the geometric multigrid preconditioner
   e2e       the same metric through the C ABI with host buffers: pinned
             host -> device copies of every input and the device -> host copy
             of u inside the timed region
   roofline  the FP64 SpMV (the dominant kernel): algorithmic bytes per launch
             over its CUDA-event launch time, against MEASURED_PEAKS.json
+  precision the 96^3 high-contrast mesh: FP64 Jacobi against mixed block Jacobi
+  batch     1024 plane-strain quad meshes in one persistent launch, against
+            the single-mesh FP64 path mesh after mesh
+  serve     an open-loop Poisson request stream through the serving loop:
+            solves/s, DOF/s, p50/p99 latency, bitwise repeats
   cpu_baseline  the C restatement of the reference (oracle/sfem_oracle.c) on
             the host cores, timed on a bounded sample and scaled (see
-            ``cpu_sample``)
+            ``cpu_sample``), with a one-thread figure and the reference's
+            dense-inverse solve of the 20^3 parity problem
 
 With N > 1 (torchrun) every rank solves its own replica on its own GPU
 ("replicas only": the path has no exchange step); value sums all ranks'
@@ -206,6 +213,16 @@ def probe_fp64_peak(device):
 # CPU baseline: the C restatement of the reference, bounded sample
 # ---------------------------------------------------------------------------
 
+def _host_threads():
+    """Host cores this process may run on (the oracle is given them
+    explicitly: a launcher such as torchrun sets OMP_NUM_THREADS=1)."""
+    import os
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except AttributeError:
+        return max(1, os.cpu_count() or 1)
+
+
 def _pcg_iteration_s(K, q, iters, threads):
     """Seconds per Jacobi-PCG iteration of the oracle on K: the difference of
     a 1-iteration and an (iters + 1)-iteration solve, after a warm-up solve
@@ -226,7 +243,7 @@ def cpu_sample(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=64, sam
     Returns (DOF/s estimate for the full workload, details)."""
     from oracle import coracle
     coracle.build()
-    threads = coracle.max_threads()
+    threads = _host_threads()
     q = pkg.meshgen.jittered_cube(ne=sample_ne)
     t0 = time.perf_counter()
     K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3, nthreads=threads)
@@ -275,7 +292,7 @@ def dense_inverse_solve(pkg, sample_ne=10):
     q = pkg.meshgen.hex_problem(sample_ne, 1001, jitter=0.0, top="sin", rtol=1e-12)
     full = pkg.meshgen.parity_cube20()
     K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3,
-                         nthreads=coracle.max_threads())
+                         nthreads=_host_threads())
     colptr, rowval, nzval, _, n = K.arrays()
     del K
     import scipy.sparse as sp
@@ -310,8 +327,8 @@ def reference_arm(args, dist):
     sample_ne = min(64, ne)
     q = pkg.meshgen.jittered_cube(ne=sample_ne)
     Kq = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3,
-                          nthreads=coracle.max_threads())
-    _, st = Kq.solve(q.fixed_dofs, q.fixed_vals, rtol=args.rtol, nthreads=coracle.max_threads())
+                          nthreads=_host_threads())
+    _, st = Kq.solve(q.fixed_dofs, q.fixed_vals, rtol=args.rtol, nthreads=_host_threads())
     del Kq
     iters_full = int(round(st["iters"] * ne / sample_ne))
     vals = []
