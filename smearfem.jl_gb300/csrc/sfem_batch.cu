@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = *cl.map_shared_rank(&s_mesh, 0);
         cl.sync();
         if (q >= a.nbig) break;
-        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED, UF, WF, 1, false, false, MG>(ClusterGroup(), tab, a,
+        process_mesh<ClusterGroup, NDIM, NEN, NGP, B, MIXED, UF, WF, 1, false, MG>(ClusterGroup(), tab, a,
                                                                                        a.order[q], red, xch, &s_flag);
         cl.sync();
     }
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(512, (NDIM == 2 ? 2 : 1)) k_batch(const __grid
         const int64_t q = (int64_t)a.nbig + s_mesh;
         __syncthreads();
         if (q >= a.nmesh) break;
-        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED, UF, WF, 1, false, false, MG>(SoloGroup(), tab, a,
+        process_mesh<SoloGroup, NDIM, NEN, NGP, B, MIXED, UF, WF, 1, false, MG>(SoloGroup(), tab, a,
                                                                                     a.order[q], red, xch, &s_flag);
         __syncthreads();
     }

@@ -457,15 +457,6 @@ __device__ __forceinline__ double2 cg_update(T *__restrict__ xv, T *__restrict__
     return make_double2(prz, prr);
 }
 
-// cg_update as a separate function (see grp_spmv_call).
-template <typename T, int B, int NVF>
-__device__ __noinline__ double2 cg_update_call(T *__restrict__ xv, T *__restrict__ rv, T *__restrict__ zv,
-                                               const T *__restrict__ pv, const T *__restrict__ qv,
-                                               const T *__restrict__ minv, T alpha, int64_t n0, int64_t n1,
-                                               int64_t gt, int64_t gstride) {
-    return cg_update<T, B, NVF>(xv, rv, zv, pv, qv, minv, alpha, n0, n1, gt, gstride);
-}
-
 // One CTA working alone on a mesh.
 struct SoloGroup {
     __device__ __forceinline__ int rank() const { return 0; }
@@ -526,7 +517,7 @@ namespace sfem_dev {
 // its pipelined path (0: none), NV: nodes per thread and step of the vector
 // update.  The register budget of the calling kernel decides what fits.
 template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF = 4, int WF = 0, int NVF = 1,
-          bool SPMV_CALL = false, bool UPD_CALL = false, bool MG = false>
+          bool SPMV_CALL = false, bool MG = false>
 __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb, double *red, double *xch,
                              int *s_flag) {
     using T = typename std::conditional<MIXED, float, double>::type;
@@ -957,11 +948,7 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
             const T alpha = (T)(rz / pq);
             double prz, prr;
             {
-                double2 pr;
-                if constexpr (UPD_CALL)
-                    pr = cg_update_call<T, B, NVF>(xv, rv, zpre, pv, qv, mpre, alpha, n0, n1, gt, gstride);
-                else
-                    pr = cg_update<T, B, NVF>(xv, rv, zpre, pv, qv, mpre, alpha, n0, n1, gt, gstride);
+                const double2 pr = cg_update<T, B, NVF>(xv, rv, zpre, pv, qv, mpre, alpha, n0, n1, gt, gstride);
                 prz = pr.x;
                 prr = pr.y;
                 if constexpr (MGOK) {
@@ -1079,7 +1066,7 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
 template <class Grp, int NDIM, int NEN, int NGP, int B, bool MIXED, int UF, int WF, int NVF, bool SPMV_CALL>
 __device__ __noinline__ void process_mesh_mg(const Grp &G, const ElemTableB &tab, const BatchArgs &a, int mb,
                                              double *red, double *xch, int *s_flag) {
-    process_mesh<Grp, NDIM, NEN, NGP, B, MIXED, UF, WF, NVF, SPMV_CALL, false, true>(G, tab, a, mb, red, xch, s_flag);
+    process_mesh<Grp, NDIM, NEN, NGP, B, MIXED, UF, WF, NVF, SPMV_CALL, true>(G, tab, a, mb, red, xch, s_flag);
 }
 
 // 2D classes fit two 512-thread CTAs per SM (64 registers); 3D elasticity
