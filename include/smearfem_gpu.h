@@ -161,14 +161,20 @@ SFEM_API int sfem_assemble_system(sfem_ctx *ctx, int64_t ne, const double *NodeL
  *    a 3D elasticity hex, 40 for a 2D elasticity quad, 36 for a 3D Laplace
  *    hex) plus the Young/nu values; larger meshes get SFEM_BAD_ARG.  That is
  *    at most 25,890 hex elasticity elements with per-element Young.
- *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) for that device; make that first call before any
- *    stream capture.
+ *  - Each call looks up the array's device address (cudaGetSymbolAddress)
+ *    with the context's device current.  The first lookup on a device may
+ *    load the library's device code there, so make the first call before
+ *    any stream capture; later lookups allocate nothing, and a context
+ *    created after cudaDeviceReset gets the array's new address.
  *  - Every call, from any context, shares the one array: calls that overlap
  *    on the GPU (other streams, other host threads) race.  Calls on one
  *    context are ordered by its stream and do not.
  *  - Young/nu: length 1 or ne^ndim, in `mem_space` (host or device).  The
- *    FP32 copy of K used by SFEM_MIXED solves is refreshed too. */
+ *    FP32 copy of K used by SFEM_MIXED solves is refreshed too.
+ *  - On a non-zero return from the argument checks or the element kernel
+ *    (det J = 0, a bad index), K keeps its previous values; after any later
+ *    failure (a CUDA error in the gather or the FP32 refresh) K's values are
+ *    undefined and K should be re-assembled. */
 SFEM_API int sfem_reassemble_noalloc(sfem_ctx *ctx, sfem_matrix *K, const double *Young,
                                      int64_t nYoung, const double *nu, int64_t nNu,
                                      int mem_space);

@@ -292,6 +292,8 @@ int launch_gather(sfem_ctx *ctx, const sfem_mesh *m, const double *kbuf, double 
 int sfem_element_stiffness(sfem_ctx *ctx, const sfem_mesh *m, int plane, const double *E, int64_t nE,
                            const double *nu, int64_t nNu, double *kbuf) {
     if (m->nEl == 0) return SFEM_OK;
+    // the negative-det J count is per assembly: earlier calls on this context must not add to it
+    SFEM_CUDA(ctx, cudaMemsetAsync(&ctx->d_err->neg_det, 0, sizeof(ctx->d_err->neg_det), ctx->stream));
     if (m->fclass == SFEM_Q2) return launch_element<2, 9, 4, 1>(ctx, m, plane, E, nE, nu, nNu, kbuf);
     if (m->ndim == 2)
         return m->b == 1 ? launch_element<2, 4, 4, 1>(ctx, m, plane, E, nE, nu, nNu, kbuf)

@@ -15,8 +15,6 @@
 // ordered pool lives here in a file-scope device array instead, together
 // with the copies of Young/nu.  Its size is fixed at build time
 // (SFEM_NOALLOC_SCRATCH_DOUBLES, 64 MiB); meshes that need more are rejected.
-#include <mutex>
-
 #include "sfem_internal.cuh"
 
 // 8 Mi doubles = 64 MiB on every GPU that loads the library, held until exit.
@@ -26,28 +24,20 @@ static __device__ __align__(256) double g_noalloc_scratch[SFEM_NOALLOC_SCRATCH_D
 
 namespace {
 
-constexpr int kMaxDevices = 128;
-std::mutex g_setup_mutex;
-double *g_scratch_addr[kMaxDevices] = {nullptr};  // device address of g_noalloc_scratch, per device
-
 // In host code `g_noalloc_scratch` names a host-side stand-in, not device
-// memory, so its device address is looked up once per device (with that
-// device current) and cached.
+// memory, so its device address is looked up with the device current.  The
+// first lookup on a device may load the module (do it before any stream
+// capture); later lookups allocate nothing and are repeated on every call,
+// so a context rebuilt after cudaDeviceReset gets the array's new address.
 int scratch_for_device(sfem_ctx *ctx, double **out) {
-    const int dev = ctx->device;
-    if (dev < 0 || dev >= kMaxDevices) return sfem_set_error(ctx, SFEM_BAD_ARG, "device ordinal %d too large", dev);
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            cudaGetLastError();
-            return sfem_set_error(ctx, SFEM_CUDA_ERROR, "cudaGetSymbolAddress(no-alloc scratch): %s",
-                                  cudaGetErrorString(e));
-        }
-        g_scratch_addr[dev] = (double *)p;
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        return sfem_set_error(ctx, SFEM_CUDA_ERROR, "cudaGetSymbolAddress(no-alloc scratch): %s",
+                              cudaGetErrorString(e));
     }
-    *out = g_scratch_addr[dev];
+    *out = (double *)p;
     return SFEM_OK;
 }
 
@@ -99,6 +89,9 @@ extern "C" int sfem_reassemble_noalloc(sfem_ctx *ctx, sfem_matrix *K, const doub
     // Every scratch entry the gather reads is written by the element kernel of
     // this same call, so nothing in the shared array has to be cleared first.
     SFEM_TRY(sfem_element_stiffness(ctx, m, K->plane, dE, nYoung, dnu, nNu, kbuf));
+    // Errors of the element kernel (det J = 0, a bad index) are reported
+    // before anything is written into K, so K keeps its old values then.
+    SFEM_TRY(sfem_check_device(ctx, "no-alloc element stiffness"));
     SFEM_TRY(sfem_gather_blocks(ctx, m, kbuf, K->val, nullptr));
     if (K->val32) {  // keep the FP32 copy used by the mixed solver consistent
         const int64_t nv = m->nslabs * 32 * b * b;
