@@ -56,6 +56,19 @@ def lib():
         L.oc_solve_pcg.argtypes = [P, i64p, C.c_int64, f64p, P, C.c_double, C.c_int, C.c_int,
                                    f64p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double)]
+        L.oc_solve_pcg_mark.restype = C.c_int
+        L.oc_solve_pcg_mark.argtypes = [P, i64p, C.c_int64, f64p, P, C.c_double, C.c_int, C.c_int,
+                                        f64p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_int),
+                                        C.POINTER(C.c_double)]
+        L.oc_pcg_begin.restype = P
+        L.oc_pcg_begin.argtypes = [P, i64p, C.c_int64, f64p, P, C.c_int]
+        L.oc_pcg_run.restype = C.c_int
+        L.oc_pcg_run.argtypes = [P, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double)]
+        L.oc_pcg_end.restype = C.c_int
+        L.oc_pcg_end.argtypes = [P, f64p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double)]
         L.oc_max_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -84,7 +97,11 @@ class OracleCSC:
         return colptr, rowval, nzval, m.value, n.value
 
     def solve(self, fixed_dofs, fixed_vals, f=None, rtol=1e-13, maxit=200000, nthreads=0,
-              max_iters=None):
+              max_iters=None, mark_rtol=None):
+        """Jacobi-PCG on the eliminated system.  With ``mark_rtol`` the stats
+        also hold ``mark_iters`` / ``mark_s``: the iteration and the seconds
+        since the solve started at which the relative residual first reached
+        ``mark_rtol`` (a looser solve's cost, measured inside this one)."""
         m, n, nnz = C.c_int64(), C.c_int64(), C.c_int64()
         lib().oc_csc_info(self.h, C.byref(m), C.byref(n), C.byref(nnz))
         u = np.empty(n.value)
@@ -97,10 +114,48 @@ class OracleCSC:
         if f is not None:
             f = np.ascontiguousarray(f, dtype=np.float64)
             fp = f.ctypes.data
-        st = lib().oc_solve_pcg(self.h, fx, fx.size, fv, fp, rtol,
-                                max_iters if max_iters else maxit, nthreads, u,
-                                C.byref(it), C.byref(rr), C.byref(ts))
-        return u, dict(status=st, iters=it.value, relres=rr.value, seconds=ts.value)
+        mi, ms = C.c_int(-1), C.c_double(0.0)
+        st = lib().oc_solve_pcg_mark(self.h, fx, fx.size, fv, fp, rtol,
+                                     max_iters if max_iters else maxit, nthreads, u,
+                                     C.byref(it), C.byref(rr), C.byref(ts),
+                                     float(mark_rtol or 0.0), C.byref(mi), C.byref(ms))
+        out = dict(status=st, iters=it.value, relres=rr.value, seconds=ts.value)
+        if mark_rtol:
+            out.update(mark_iters=mi.value, mark_s=ms.value)
+        return u, out
+
+
+class PcgSolve:
+    """The oracle's Jacobi-PCG split into resumable pieces: ``run`` performs up
+    to ``max_iters`` more iterations (the iterations of one uninterrupted
+    solve), ``finish`` returns ``(u, stats)`` and frees the state."""
+
+    def __init__(self, K, fixed_dofs, fixed_vals, f=None, nthreads=0):
+        self.K = K  # keeps the matrix alive while the solve runs
+        m, n, nnz = C.c_int64(), C.c_int64(), C.c_int64()
+        lib().oc_csc_info(K.h, C.byref(m), C.byref(n), C.byref(nnz))
+        self.n = n.value
+        fx = np.ascontiguousarray(fixed_dofs, dtype=np.int64)
+        fv = np.ascontiguousarray(fixed_vals, dtype=np.float64)
+        fp = None
+        if f is not None:
+            self._f = np.ascontiguousarray(f, dtype=np.float64)
+            fp = self._f.ctypes.data
+        self.s = lib().oc_pcg_begin(K.h, fx, fx.size, fv, fp, int(nthreads))
+        self.mark_iters, self.mark_s = C.c_int(-1), C.c_double(0.0)
+
+    def run(self, max_iters, rtol, mark_rtol=0.0):
+        """Returns 0 once converged, 1 while iterations remain, 2 on a zero diagonal."""
+        return int(lib().oc_pcg_run(self.s, int(max_iters), float(rtol), float(mark_rtol),
+                                    C.byref(self.mark_iters), C.byref(self.mark_s)))
+
+    def finish(self):
+        u = np.empty(self.n)
+        it, rr, ts = C.c_int(), C.c_double(), C.c_double()
+        st = lib().oc_pcg_end(self.s, u, C.byref(it), C.byref(rr), C.byref(ts))
+        self.s = None
+        return u, dict(status=st, iters=it.value, relres=rr.value, seconds=ts.value,
+                       mark_iters=self.mark_iters.value, mark_s=self.mark_s.value)
 
 
 def assemble(ne, NodeList, IEN, ndim, FunctionClass="Q1", nDof=1, ID=None, Young=1.0,

@@ -17,7 +17,8 @@
  *   oc_solve_pcg  examples/vector3D.jl:315-322 with the dense inverse of
  *                 K_free replaced by Jacobi-preconditioned CG on the free
  *                 DOFs (the dense inverse is O(n_f^3) and infeasible beyond a
- *                 few 10^4 DOFs).  q = q_d + C q_f.
+ *                 few 10^4 DOFs).  q = q_d + C q_f.  oc_pcg_begin / _run /
+ *                 _end split the same solve into resumable pieces.
  *
  * Element work runs in parallel over elements (OpenMP) when nthreads > 1;
  * each element owns its COO slots, so results do not depend on the thread
@@ -340,13 +341,52 @@ void oc_free(void *h) {
     free(K);
 }
 
-/* CSR of K (transpose of the stored CSC), 0-based */
+/* CSR of K (transpose of the stored CSC), 0-based.  K's pattern is
+ * symmetric (every element writes the full node-pair block), so row i of the
+ * CSR has the pattern of column i, and entry (i, j) of column j goes to the
+ * position of j in column i's sorted row list: each column is transposed
+ * independently (parallel, no conflicts).  A non-symmetric pattern takes the
+ * serial counting transposition. */
+static int64_t find_sorted(const int64_t *a, int64_t lo, int64_t hi, int64_t v) {
+    while (lo < hi) {
+        int64_t mid = lo + (hi - lo) / 2;
+        if (a[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
 static void build_csr(oc_csc *K) {
     if (K->rp) return;
     int64_t n = K->n, m = K->m, nnz = K->nnz;
     K->rp = (int64_t *)calloc((size_t)m + 1, sizeof(int64_t));
     K->cj = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nnz ? nnz : 1));
     K->rv = (double *)malloc(sizeof(double) * (size_t)(nnz ? nnz : 1));
+    int sym = (m == n);
+    if (sym) {
+        int bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad)
+#endif
+        for (int64_t j = 0; j < n; ++j) {
+            for (int64_t k = K->colptr[j] - 1; k < K->colptr[j + 1] - 1; ++k) {
+                int64_t i = K->rowval[k] - 1; /* entry (i, j) */
+                int64_t a = K->colptr[i] - 1, b = K->colptr[i + 1] - 1;
+                int64_t q = find_sorted(K->rowval, a, b, j + 1);
+                if (q >= b || K->rowval[q] != j + 1) {
+                    bad = 1;
+                    continue;
+                }
+                K->cj[q] = j;
+                K->rv[q] = K->nzval[k];
+            }
+        }
+        if (!bad) {
+            for (int64_t i = 0; i <= m; ++i) K->rp[i] = K->colptr[i] - 1;
+            return;
+        }
+        memset(K->rp, 0, sizeof(int64_t) * (size_t)(m + 1));
+    }
     for (int64_t k = 0; k < nnz; ++k) K->rp[K->rowval[k]]++;
     for (int64_t i = 0; i < m; ++i) K->rp[i + 1] += K->rp[i];
     int64_t *cur = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m + 1));
@@ -385,83 +425,153 @@ static double dot(int64_t n, const double *a, const double *b, int nth) {
 
 /*
  * Dirichlet elimination + Jacobi-PCG (examples/vector3D.jl:315-322 with the
- * dense inverse replaced).  fixed: 1-based DOF ids.  Returns 0 on success,
- * 1 if maxit was reached, 2 on a zero diagonal at a free DOF.
- * If max_iters_timed > 0 the solve stops after that many iterations (used to
- * time a bounded sample); the status is then 1.
+ * dense inverse replaced), as a resumable solve:
+ *   oc_pcg_begin  lift (r = C'(f - K q_d)), Jacobi diagonal, z = M^-1 r, p = z
+ *   oc_pcg_run    up to max_iters more CG iterations, or until the relative
+ *                 residual is at or below rtol
+ *   oc_pcg_end    q = q_d + C q_f, statistics, frees the state
+ * Splitting a solve into several oc_pcg_run calls performs exactly the
+ * iterations of one call.  fixed: 1-based DOF ids.
  */
-int oc_solve_pcg(void *h, const int64_t *fixed, int64_t nfix, const double *vals,
-                 const double *f, double rtol, int maxit, int nthreads, double *u,
-                 int *iters, double *relres, double *t_solve) {
+typedef struct {
+    oc_csc *K;
+    int64_t n;
+    int nth, it, status; /* status: 0 converged, 1 running / maxit, 2 zero diagonal */
+    unsigned char *fx;
+    double *ud, *r, *z, *p, *q, *x, *dinv;
+    double bb, rr, rz, t0;
+} oc_pcg;
+
+void *oc_pcg_begin(void *h, const int64_t *fixed, int64_t nfix, const double *vals,
+                   const double *f, int nthreads) {
+    oc_pcg *S = (oc_pcg *)calloc(1, sizeof(oc_pcg));
     oc_csc *K = (oc_csc *)h;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-    double t0 = now_s();
+    S->t0 = now_s();
+    S->K = K;
+    S->nth = nthreads;
     build_csr(K);
-    int64_t n = K->n;
-    unsigned char *fx = (unsigned char *)calloc((size_t)n, 1);
-    double *ud = (double *)calloc((size_t)n, sizeof(double));
+    int64_t n = S->n = K->n;
+    S->fx = (unsigned char *)calloc((size_t)n, 1);
+    S->ud = (double *)calloc((size_t)n, sizeof(double));
     for (int64_t k = 0; k < nfix; ++k) {
-        fx[fixed[k] - 1] = 1;
-        ud[fixed[k] - 1] = vals[k];
+        S->fx[fixed[k] - 1] = 1;
+        S->ud[fixed[k] - 1] = vals[k];
     }
-    double *r = (double *)malloc(sizeof(double) * (size_t)n);
-    double *z = (double *)malloc(sizeof(double) * (size_t)n);
-    double *p = (double *)malloc(sizeof(double) * (size_t)n);
-    double *q = (double *)malloc(sizeof(double) * (size_t)n);
-    double *x = (double *)calloc((size_t)n, sizeof(double));
-    double *dinv = (double *)calloc((size_t)n, sizeof(double));
+    S->r = (double *)malloc(sizeof(double) * (size_t)n);
+    S->z = (double *)malloc(sizeof(double) * (size_t)n);
+    S->p = (double *)malloc(sizeof(double) * (size_t)n);
+    S->q = (double *)malloc(sizeof(double) * (size_t)n);
+    S->x = (double *)calloc((size_t)n, sizeof(double));
+    S->dinv = (double *)calloc((size_t)n, sizeof(double));
+    unsigned char *fx = S->fx;
+    double *dinv = S->dinv;
     int status = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : status) if (nthreads > 1)
+#endif
     for (int64_t i = 0; i < n; ++i) {
         if (fx[i]) continue;
         double d = 0;
         for (int64_t k = K->rp[i]; k < K->rp[i + 1]; ++k)
             if (K->cj[k] == i) d += K->rv[k];
-        if (d == 0) status = 2;
+        if (d == 0) status |= 2;
         dinv[i] = d != 0 ? 1.0 / d : 0.0;
     }
-    spmv(K, ud, q, fx, nthreads);
-    for (int64_t i = 0; i < n; ++i) r[i] = fx[i] ? 0.0 : (f ? f[i] : 0.0) - q[i];
-    double bb = dot(n, r, r, nthreads);
-    int it = 0;
-    double rr = bb;
-    if (status == 0 && bb > 0) {
-        for (int64_t i = 0; i < n; ++i) { z[i] = dinv[i] * r[i]; p[i] = z[i]; }
-        double rz = dot(n, r, z, nthreads);
+    spmv(K, S->ud, S->q, fx, nthreads);
+    for (int64_t i = 0; i < n; ++i) S->r[i] = fx[i] ? 0.0 : (f ? f[i] : 0.0) - S->q[i];
+    S->bb = S->rr = dot(n, S->r, S->r, nthreads);
+    if (status == 0 && S->bb > 0) {
+        for (int64_t i = 0; i < n; ++i) { S->z[i] = dinv[i] * S->r[i]; S->p[i] = S->z[i]; }
+        S->rz = dot(n, S->r, S->z, nthreads);
         status = 1;
-        for (it = 0; it < maxit;) {
-            spmv(K, p, q, fx, nthreads);
-            double alpha = rz / dot(n, p, q, nthreads);
-            double rzn = 0, rrn = 0;
-            (void)rzn;
+    }
+    S->status = status;
+    return S;
+}
+
+/* Returns the status (0 once converged).  mark_rtol > 0: the first
+ * iteration at which the relative residual is at or below mark_rtol, and
+ * the seconds since oc_pcg_begin started, go to *mark_iters / *mark_s (left
+ * alone while it is not reached, so *mark_iters starts at -1). */
+int oc_pcg_run(void *state, int max_iters, double rtol, double mark_rtol, int *mark_iters,
+               double *mark_s) {
+    oc_pcg *S = (oc_pcg *)state;
+    const int64_t n = S->n;
+    const int nthreads = S->nth;
+    double *x = S->x, *r = S->r, *z = S->z, *p = S->p, *q = S->q, *dinv = S->dinv;
+    if (S->status != 1) return S->status;
+    if (S->rr <= rtol * rtol * S->bb) { S->status = 0; return 0; }
+    for (int k = 0; k < max_iters; ++k) {
+        spmv(S->K, p, q, S->fx, nthreads);
+        double alpha = S->rz / dot(n, p, q, nthreads);
+        double rzn = 0, rrn = 0;
 #ifdef _OPENMP
 #pragma omp parallel for reduction(+ : rzn, rrn) schedule(static) if (nthreads > 1)
 #endif
-            for (int64_t i = 0; i < n; ++i) {
-                x[i] += alpha * p[i];
-                r[i] -= alpha * q[i];
-                z[i] = dinv[i] * r[i];
-                rzn += r[i] * z[i];
-                rrn += r[i] * r[i];
-            }
-            ++it;
-            rr = rrn;
-            if (rr <= rtol * rtol * bb) { status = 0; break; }
-            double beta = rzn / rz;
-            rz = rzn;
+        for (int64_t i = 0; i < n; ++i) {
+            x[i] += alpha * p[i];
+            r[i] -= alpha * q[i];
+            z[i] = dinv[i] * r[i];
+            rzn += r[i] * z[i];
+            rrn += r[i] * r[i];
+        }
+        ++S->it;
+        S->rr = rrn;
+        if (mark_rtol > 0 && mark_iters && *mark_iters < 0 && S->rr <= mark_rtol * mark_rtol * S->bb) {
+            *mark_iters = S->it;
+            if (mark_s) *mark_s = now_s() - S->t0;
+        }
+        if (S->rr <= rtol * rtol * S->bb) { S->status = 0; return 0; }
+        double beta = rzn / S->rz;
+        S->rz = rzn;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) if (nthreads > 1)
 #endif
-            for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
-        }
+        for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
     }
-    for (int64_t i = 0; i < n; ++i) u[i] = ud[i] + x[i];
-    if (iters) *iters = it;
-    if (relres) *relres = bb > 0 ? sqrt(rr / bb) : 0.0;
-    if (t_solve) *t_solve = now_s() - t0;
-    free(fx); free(ud); free(r); free(z); free(p); free(q); free(x); free(dinv);
+    return S->status;
+}
+
+int oc_pcg_end(void *state, double *u, int *iters, double *relres, double *t_solve) {
+    oc_pcg *S = (oc_pcg *)state;
+    int status = S->status;
+    for (int64_t i = 0; i < S->n; ++i) u[i] = S->ud[i] + S->x[i];
+    if (iters) *iters = S->it;
+    if (relres) *relres = S->bb > 0 ? sqrt(S->rr / S->bb) : 0.0;
+    if (t_solve) *t_solve = now_s() - S->t0;
+    free(S->fx); free(S->ud); free(S->r); free(S->z); free(S->p); free(S->q); free(S->x);
+    free(S->dinv);
+    free(S);
     return status;
+}
+
+/* The whole solve in one call.  Returns 0 on success, 1 if maxit was reached,
+ * 2 on a zero diagonal at a free DOF; mark_rtol as in oc_pcg_run
+ * (*mark_iters = -1 if it was never reached). */
+int oc_solve_pcg_mark(void *h, const int64_t *fixed, int64_t nfix, const double *vals,
+                      const double *f, double rtol, int maxit, int nthreads, double *u,
+                      int *iters, double *relres, double *t_solve, double mark_rtol,
+                      int *mark_iters, double *mark_s) {
+    if (mark_iters) *mark_iters = -1;
+    if (mark_s) *mark_s = 0.0;
+    void *S = oc_pcg_begin(h, fixed, nfix, vals, f, nthreads);
+    oc_pcg *P = (oc_pcg *)S;
+    if (P->status == 1 && mark_rtol > 0 && P->rr <= mark_rtol * mark_rtol * P->bb && mark_iters) {
+        *mark_iters = 0;
+        if (mark_s) *mark_s = now_s() - P->t0;
+    }
+    oc_pcg_run(S, maxit, rtol, mark_rtol, mark_iters, mark_s);
+    return oc_pcg_end(S, u, iters, relres, t_solve);
+}
+
+int oc_solve_pcg(void *h, const int64_t *fixed, int64_t nfix, const double *vals,
+                 const double *f, double rtol, int maxit, int nthreads, double *u,
+                 int *iters, double *relres, double *t_solve) {
+    return oc_solve_pcg_mark(h, fixed, nfix, vals, f, rtol, maxit, nthreads, u, iters, relres,
+                             t_solve, 0.0, NULL, NULL);
 }
 
 int oc_max_threads(void) {
