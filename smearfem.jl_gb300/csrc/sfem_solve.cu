@@ -174,7 +174,9 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
 }
 
 // The same product from the upper-triangle copy (sfem_sym.cu):
-// y_r = sum_{c>=r} A_rc x_c + sum_{c<r} A_cr^T x_c, one lane per row.
+// y_r = sum_{c>=r} A_rc x_c + sum_{c<r} A_cr^T x_c, one lane per row, the
+// upper part first, then the lower part, each in a fixed order (the result
+// is deterministic).
 // FUSE: the multiplied vector is the new CG direction p = z + beta x
 // (x = the previous direction), formed on the fly from the gathered entries;
 // each lane stores its own rows of p to pout.  This replaces the separate
@@ -183,13 +185,24 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
 // SPMV_SMOOTH stores y = x + Mv (bv - K x) (Mv: the smoother's b x b blocks)
 // and, with MODE 3, reduces bv.y into rz and sets beta = rz / rz_prev.
 // Both skip once the solve is done.
-template <typename T, int B, int MODE, bool FUSE = false, int EPI = sfem_dev::SPMV_Y>
+//
+// Traffic.  Every upper block is read twice: by its own row and, transposed,
+// by its column's row.  Both reads come from DRAM only once if the second
+// follows the first while the block is still in L2, i.e. if the slices in
+// flight at any moment hold less than the L2.  So the grid is persistent (the
+// CTAs that fit at once, striding over the slices in order) and each lane
+// keeps U blocks of its row in flight, with the next batch's column indices
+// (lower entries) already loaded: about 24 warps per SM cover the memory
+// latency, and the open slices (~3.6k at 128^3, ~75 MB) stay well inside the
+// L2.  A one-slice-per-warp grid kept ~10k slices (~200 MB) open and read
+// 19-26% more than the algorithmic bytes.
+template <typename T, int B, int MODE, bool FUSE = false, int EPI = sfem_dev::SPMV_Y, int U = 4>
 __global__ void __launch_bounds__(SPMV_T)
 k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, const T *__restrict__ valU,
-           const int64_t *__restrict__ sptrL, const int2 *__restrict__ lo, int64_t nN, int64_t nslices,
-           const T *__restrict__ x, T *__restrict__ y, const unsigned char *__restrict__ fixed, CgScalars *S,
-           double *partial, const T *__restrict__ z = nullptr, T *__restrict__ pout = nullptr,
-           const T *__restrict__ bv = nullptr, const T *__restrict__ Mv = nullptr) {
+            const int64_t *__restrict__ sptrL, const int2 *__restrict__ lo, int64_t nN, int64_t nslices,
+            const T *__restrict__ x, T *__restrict__ y, const unsigned char *__restrict__ fixed, CgScalars *S,
+            double *partial, const T *__restrict__ z = nullptr, T *__restrict__ pout = nullptr,
+            const T *__restrict__ bv = nullptr, const T *__restrict__ Mv = nullptr) {
     if ((MODE == 1 || MODE == 3 || EPI != sfem_dev::SPMV_Y) && S->done) return;
     const T beta = FUSE ? (T)S->beta : T(0);
     const int lane = threadIdx.x & 31;
@@ -200,49 +213,72 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
         T acc[B];
 #pragma unroll
         for (int i = 0; i < B; ++i) acc[i] = T(0);
-        // upper and lower parts in one loop: the lower part's loads depend on
-        // its index entry, the upper part's do not, so interleaving them keeps
-        // more independent loads in flight; the next index entry is prefetched.
-        // Index arrays are read once (streaming hint); the upper values are read
-        // again as a neighbour's lower blocks, so they keep the normal policy.
         const int64_t u0 = sptrU[s], nu = sptrU[s + 1] - u0;
         const int64_t l0 = sptrL[s], nl = sptrL[s + 1] - l0;
-        const int64_t nk = nu > nl ? nu : nl;
-        int2 ent_next = nl > 0 ? __ldcs(&lo[l0 * 32 + lane]) : make_int2(-1, 0);
-        for (int64_t k = 0; k < nk; ++k) {
-            const int2 ent = ent_next;
-            if (k + 1 < nl) ent_next = __ldcs(&lo[(l0 + k + 1) * 32 + lane]);
-            if (k < nu) {
-                const int64_t su = u0 + k;
-                const int c = __ldcs(&colU[su * 32 + lane]);
-                T v[B * B];
-                load_v32<B, false>(valU, su, lane, v);
-                T xc[B];
+        // upper part: A_rc x_c
+        int cn[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) cn[u] = u < nu ? __ldcs(&colU[(u0 + u) * 32 + lane]) : 0;
+        for (int64_t k0 = 0; k0 < nu; k0 += U) {
+            int c[U];
+            T v[U][B * B];
+            T xc[U][B];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                c[u] = cn[u];
+                if (k0 + u < nu) {
+                    load_v32<B, false>(valU, u0 + k0 + u, lane, v[u]);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < B * B; ++e) v[u][e] = T(0);
+                }
 #pragma unroll
                 for (int j = 0; j < B; ++j) {
-                    xc[j] = __ldg(&x[(int64_t)c * B + j]);
-                    if (FUSE) xc[j] = fma(beta, xc[j], __ldg(&z[(int64_t)c * B + j]));
+                    xc[u][j] = __ldg(&x[(int64_t)c[u] * B + j]);
+                    if (FUSE) xc[u][j] = fma(beta, xc[u][j], __ldg(&z[(int64_t)c[u] * B + j]));
                 }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) cn[u] = k0 + U + u < nu ? __ldcs(&colU[(u0 + k0 + U + u) * 32 + lane]) : 0;
+#pragma unroll
+            for (int u = 0; u < U; ++u)
 #pragma unroll
                 for (int i = 0; i < B; ++i)
 #pragma unroll
-                    for (int j = 0; j < B; ++j) acc[i] = fma(v[i * B + j], xc[j], acc[i]);
-            }
-            if (k < nl && ent.x >= 0) {  // ent.x < 0: padding
-                const int c = ent.y;
-                T v[B * B];
-                load_v32<B, false>(valU, ent.x >> 5, ent.x & 31, v);
-                T xc[B];
+                    for (int j = 0; j < B; ++j) acc[i] = fma(v[u][i * B + j], xc[u][j], acc[i]);
+        }
+        // lower part: A_cr^T x_c from c's upper storage
+        int2 en[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) en[u] = u < nl ? __ldcs(&lo[(l0 + u) * 32 + lane]) : make_int2(-1, 0);
+        for (int64_t k0 = 0; k0 < nl; k0 += U) {
+            T v[U][B * B];
+            T xc[U][B];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int2 e = en[u];
+                if (e.x >= 0) {
+                    load_v32<B, false>(valU, e.x >> 5, e.x & 31, v[u]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < B * B; ++q) v[u][q] = T(0);
+                }
+                const int c = e.x >= 0 ? e.y : 0;
 #pragma unroll
                 for (int j = 0; j < B; ++j) {
-                    xc[j] = __ldg(&x[(int64_t)c * B + j]);
-                    if (FUSE) xc[j] = fma(beta, xc[j], __ldg(&z[(int64_t)c * B + j]));
+                    xc[u][j] = __ldg(&x[(int64_t)c * B + j]);
+                    if (FUSE) xc[u][j] = fma(beta, xc[u][j], __ldg(&z[(int64_t)c * B + j]));
                 }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                en[u] = k0 + U + u < nl ? __ldcs(&lo[(l0 + k0 + U + u) * 32 + lane]) : make_int2(-1, 0);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
 #pragma unroll
                 for (int i = 0; i < B; ++i)
 #pragma unroll
-                    for (int j = 0; j < B; ++j) acc[i] = fma(v[j * B + i], xc[j], acc[i]);
-            }
+                    for (int j = 0; j < B; ++j) acc[i] = fma(v[u][j * B + i], xc[u][j], acc[i]);
         }
         if (r < nN) {
             if constexpr (EPI == sfem_dev::SPMV_Y) {
@@ -892,9 +928,12 @@ int Solver::mg_cycle(const float *r, float *z) {
     auto grid = [&](int64_t work) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(sfem_cdiv(work, 256), 8 * ctx->num_sms)); };
     const MgLevel &F0 = mg.lev[0];
     int n = 0;
-    k_spmv_sym<float, B, 0, false, SPMV_RES><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
-        K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, F0.x, F0.t, fixed, S, partial, nullptr,
-        nullptr, r, nullptr);
+    {
+        auto kern = k_spmv_sym<float, B, 0, false, SPMV_RES>;
+        kern<<<resident_grid(ctx, kern, SPMV_T, spmv_grid), SPMV_T, 0, ctx->stream>>>(
+            K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, F0.x, F0.t, fixed, S, partial, nullptr,
+            nullptr, r, nullptr);
+    }
     ++n;
     for (int l = 1; l < L; ++l) {
         k_mg_restrict<NDIM, B><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mgM, mg.lev[l - 1], mg.lev[l], l - 1,
@@ -916,9 +955,12 @@ int Solver::mg_cycle(const float *r, float *z) {
         xin = mg.lev[l].t;
     }
     k_mg_prolong<NDIM, B><<<grid(F0.nnode), 256, 0, ctx->stream>>>(mga, mgM, F0, mg.lev[1], 0, xin, S);
-    k_spmv_sym<float, B, 3, false, SPMV_SMOOTH><<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
-        K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, F0.x, z, fixed, S, partial, nullptr,
-        nullptr, r, F0.minv);
+    {
+        auto kern = k_spmv_sym<float, B, 3, false, SPMV_SMOOTH>;
+        kern<<<resident_grid(ctx, kern, SPMV_T, spmv_grid), SPMV_T, 0, ctx->stream>>>(
+            K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, F0.x, z, fixed, S, partial, nullptr,
+            nullptr, r, F0.minv);
+    }
     n += 2;
     ctx->launches += n;
     mg_launches = n;
@@ -931,12 +973,12 @@ void Solver::launch_spmv(const T *val, const T *x, T *y, bool fused) {
         if (K->sym_state == 1 && opts.fp32_storage == SFEM_FP32_UPPER) {
             if (fused) {
                 auto kern = k_spmv_sym<float, B, 1>;
-                kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+                kern<<<resident_grid(ctx, kern, SPMV_T, spmv_grid), SPMV_T, 0, ctx->stream>>>(
                     K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial,
                     nullptr, nullptr, nullptr, nullptr);
             } else {
                 auto kern = k_spmv_sym<float, B, 0>;
-                kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(
+                kern<<<resident_grid(ctx, kern, SPMV_T, spmv_grid), SPMV_T, 0, ctx->stream>>>(
                     K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN, m->nslices, x, y, fixed, S, partial,
                     nullptr, nullptr, nullptr, nullptr);
             }
@@ -988,7 +1030,8 @@ int Solver::cg_loop(Vecs<T> &v, double *x64, double *r64, double *q64) {
                 T *pin = (slot % 2 == 0) ? v.p : p2, *pout = (slot % 2 == 0) ? p2 : v.p;
                 if (profile) cudaEventRecord(events[2 * slot], ctx->stream);
                 auto kern = k_spmv_sym<float, B, 1, true>;
-                kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN,
+                kern<<<resident_grid(ctx, kern, SPMV_T, spmv_grid), SPMV_T, 0, ctx->stream>>>(
+                    K->sptrU, K->colU, K->valU, K->sptrL, K->lo, m->nN,
                                                              m->nslices, pin, v.q, fixed, S, partial, v.z, pout,
                                                              nullptr, nullptr);
                 SFEM_LAUNCHED(ctx);
