@@ -9,32 +9,51 @@ seeded 4-mode z-displacement on the top face.  A step is the whole path:
 mesh upload/validation, device sparsity pattern, FP64 element stiffness and
 assembly, Dirichlet elimination and Jacobi-PCG to 1e-10 relative residual.
 
-  value     DOF / step time, inputs already resident in HBM (FP64 path)
+  oracle    the C restatement of the reference (oracle/sfem_oracle.c) runs
+            the same 128^3 problem end to end on all host cores: assembly
+            (element loop + COO -> CSC), Dirichlet lift, Jacobi-PCG to
+            1e-13, with the time at which the residual first reached 1e-10.
+            Its displacement is the reference every GPU leg's error is
+            measured against, and its time to 1e-10 is the CPU baseline.
+  value     DOF / step time, inputs already resident in HBM, FP64 path as
+            users run it (each chunk of CG iterations is one CUDA graph)
+  roofline  the FP64 SpMV (the dominant kernel): algorithmic bytes per launch
+            over its CUDA-event launch time, taken in a separate profiled
+            pass of the same step (kernels enqueued one by one, events
+            around every SpMV), against MEASURED_PEAKS.json
   mixed     the same step with the FP32-inner / FP64-refresh solver, with
             block Jacobi and with the geometric multigrid preconditioner
   e2e       the same metric through the C ABI with host buffers: pinned
             host -> device copies of every input and the device -> host copy
             of u inside the timed region
-  roofline  the FP64 SpMV (the dominant kernel): algorithmic bytes per launch
-            over its CUDA-event launch time, against MEASURED_PEAKS.json
-  precision the 96^3 high-contrast mesh: FP64 Jacobi against mixed block Jacobi
-  batch     1024 plane-strain quad meshes in one persistent launch, against
-            the single-mesh FP64 path mesh after mesh
-  serve     an open-loop Poisson request stream through the serving loop:
-            solves/s, DOF/s, p50/p99 latency, bitwise repeats
-  cpu_baseline  the C restatement of the reference (oracle/sfem_oracle.c) on
-            the host cores, timed on a bounded sample and scaled (see
-            ``cpu_sample``), with a one-thread figure and the reference's
-            dense-inverse solve of the 20^3 parity problem
+  precision the 96^3 high-contrast mesh: FP64 Jacobi against mixed block
+            Jacobi (and multigrid), errors against the oracle's 96^3 solve
+  batch     1024 plane-strain quad meshes in one persistent launch: FP64 and
+            mixed block Jacobi and mixed multigrid on equal terms (precision
+            factor, preconditioner factor, both), errors against the
+            oracle's sparse-direct solves of sampled meshes
+  serve     an open-loop Poisson stream of freshly drawn requests through the
+            serving loop: solves/s, DOF/s, p50/p99 latency (saturated and at
+            half capacity), topology-cache hits, cold-topology latency; FP64
+            and mixed servers on one request set; a pooled bitwise-repeat
+            check; errors against the oracle on sampled requests
+  cpu_baseline  from the oracle run above (measured, not extrapolated), with
+            one-thread and dense-inverse figures beside it (estimates)
+
+--impl reference runs the reference's algorithm (the C port) on the host
+cores: its K timed steps together are ONE full run of the 128^3 workload
+(step 1 the assembly, the others the PCG iterations in chunks, the last to
+1e-10), so the value is measured on the stated workload.
 
 With N > 1 (torchrun) every rank solves its own replica on its own GPU
 ("replicas only": the path has no exchange step); value sums all ranks'
-DOFs over the max-over-ranks time.
+DOFs over the max-over-ranks time.  The oracle legs run at N = 1 only.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -56,6 +75,10 @@ FALLBACK_HBM_GBS = 6800.0
 # ncu capture of the 64^3 instance: 581.4 MB for 64,701,513 stored entries; the traffic grows
 # with the number of stored entries, so a launch at another size moves nnz times this.
 SPMV64_TRAFFIC_PER_NNZ = 581.4e6 / 64701513
+# Host memory the oracle's full run needs per element of a 3D elasticity hex mesh: the
+# reference's COO triplets (576 x 24 B), their row-bucketed copy (576 x 16 B), the CSC
+# and its CSR copy (about 2 x 245 x 16 B); 128^3 needs about 58 GB.
+ORACLE_BYTES_PER_HEX = 576 * 40 + 2 * 245 * 16
 
 
 def parse_args(argv=None):
@@ -66,27 +89,31 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ne", type=int, default=128)
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--legs", default="value,mixed,e2e,cpu,precision,batch,serve",
-                    help="comma list of value,mixed,e2e,cpu,precision,batch,serve (profiling runs pick one)")
+    ap.add_argument("--legs", default="oracle,value,mixed,e2e,precision,batch,serve,cpu",
+                    help="comma list of oracle,value,mixed,e2e,precision,batch,serve,cpu")
+    ap.add_argument("--leg-steps", type=int, default=3,
+                    help="timed steps of the mixed, precision and batch legs (value and e2e use --steps)")
+    ap.add_argument("--leg-warmup", type=int, default=2, help="warm-up steps of those legs")
     ap.add_argument("--precision-ne", type=int, default=96, help="mesh size of the precision leg")
     ap.add_argument("--batch-count", type=int, default=1024, help="meshes in the batch leg")
     ap.add_argument("--batch-launch", default="",
                     help="threads,ctas_per_sm,cluster,cluster_min_nodes: fixed batch launch shape (no autotune)")
     ap.add_argument("--batch-rtol", type=float, default=1e-12,
-                    help="batch-leg relative residual (1e-12 keeps the error in u under 1e-8)")
+                    help="batch/serve relative residual (1e-12 keeps the error in u under 1e-8)")
+    ap.add_argument("--batch-arms", default="fp64_block_jacobi,mixed_block_jacobi,mixed_multigrid",
+                    help="batch-leg solver arms (precision_precond)")
     ap.add_argument("--mixed-precond", default="both", choices=["both", "block_jacobi", "multigrid"],
                     help="preconditioners of the mixed leg (profiling runs pick one)")
     ap.add_argument("--mg-delta", type=float, default=0.01,
                     help="reliable-update factor of the multigrid solves (mixed, batch, serve): multigrid drops "
                          "the FP32 residual 10x in 2-3 iterations; 0.01 halves the FP64 refreshes at the same error")
-    ap.add_argument("--batch-precond", default="multigrid", choices=["multigrid", "block_jacobi"],
-                    help="batch-leg preconditioner (multigrid: structured meshes)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
-    ap.add_argument("--serve-requests", type=int, default=960, help="requests in the saturating stream")
-    ap.add_argument("--serve-pool", type=int, default=96, help="distinct meshes the stream draws from")
-    ap.add_argument("--serve-precond", default="multigrid", choices=["multigrid", "block_jacobi"],
-                    help="serving preconditioner (multigrid: structured meshes, cached per topology)")
+    ap.add_argument("--serve-requests", type=int, default=960, help="requests in the configured-rate stream")
+    ap.add_argument("--serve-compare", type=int, default=96,
+                    help="requests of the FP64 / mixed server comparison (submitted at once)")
     ap.add_argument("--serve-launch", default="8,256", help="cluster,threads of the serving kernel")
+    ap.add_argument("--oracle-samples", type=int, default=16,
+                    help="batch meshes / served requests whose error is measured against the oracle")
     ap.add_argument("--no-extras", action="store_true", help="same as --legs value")
     a = ap.parse_args(argv)
     a.legs = {"value"} if a.no_extras else set(x.strip() for x in a.legs.split(",") if x.strip())
@@ -198,35 +225,110 @@ def measured_peaks():
 
 
 def probe_fp64_peak(device):
+    """FP64 FMA, FP32 FMA and FP64 tensor-core (DMMA, mma.sync m8n8k4) rates
+    measured on this GPU (smearfem.jl_gb300/probe/peaks.cu), TFLOP/s."""
     import ctypes
     path = os.path.join(GE.PKG_DIR, "lib", "libsfem_probe.so")
     if not os.path.exists(path):
-        return None, None
+        return None, None, None
     L = ctypes.CDLL(path)
-    t64, t32 = ctypes.c_double(), ctypes.c_double()
+    t64, t32, tmma = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     ok = L.sfem_probe_fp64_tflops(device, ctypes.byref(t64)) == 0
     ok &= L.sfem_probe_fp32_tflops(device, ctypes.byref(t32)) == 0
-    return (t64.value, t32.value) if ok else (None, None)
+    mma = tmma.value if L.sfem_probe_dmma_tflops(device, ctypes.byref(tmma)) == 0 else None
+    return (t64.value, t32.value, mma) if ok else (None, None, None)
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the C restatement of the reference, bounded sample
+# The oracle: the C restatement of the reference on the host cores.  It is the
+# checker of every leg and, timed, the CPU baseline.  Only this section, the
+# reference arm and the cpu_baseline figures execute oracle/ code.
 # ---------------------------------------------------------------------------
 
 def _host_threads():
     """Host cores this process may run on (the oracle is given them
     explicitly: a launcher such as torchrun sets OMP_NUM_THREADS=1)."""
-    import os
     try:
         return max(1, len(os.sched_getaffinity(0)))
     except AttributeError:
         return max(1, os.cpu_count() or 1)
 
 
+def _host_available_gb():
+    """Free host memory (MemAvailable, capped by a cgroup limit)."""
+    avail = float("inf")
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable"):
+                avail = int(line.split()[1]) / 1e6
+    except OSError:
+        pass
+    for path in ("/sys/fs/cgroup/memory.max", "/sys/fs/cgroup/memory/memory.limit_in_bytes"):
+        try:
+            v = open(path).read().strip()
+            if v != "max":
+                avail = min(avail, int(v) / 1e9)
+            break
+        except (OSError, ValueError):
+            continue
+    return avail
+
+
+def _oracle_fits(n_elem):
+    need = ORACLE_BYTES_PER_HEX * n_elem / 1e9 + 2.0
+    avail = _host_available_gb()
+    return avail >= 1.5 * need, need, avail
+
+
+def oracle_full_run(p, threads, rtol=1e-13, mark=1e-10):
+    """The reference's path for problem p on the host: assembly (element loop
+    + COO -> CSC, src/fem.jl:135-256), Dirichlet lift and Jacobi-PCG
+    (examples/vector3D.jl:315-322 with the dense inverse replaced) to
+    ``rtol``, recording when the residual first reached ``mark``.  Returns
+    (u, record); record["cpu_s"] = assembly + solve time to ``mark``."""
+    from oracle import coracle
+    coracle.build()
+    nu = p.nu if np.size(p.nu) > 1 else float(p.nu[0])
+    t0 = time.perf_counter()
+    K = coracle.assemble(p.ne, p.NodeList, p.IEN, p.ndim, "Q1", p.ndim, p.ID, p.Young, nu,
+                         plane=p.plane, nthreads=threads)
+    t_asm = time.perf_counter() - t0
+    u, st = K.solve(p.fixed_dofs, p.fixed_vals, rtol=rtol, nthreads=threads, mark_rtol=mark)
+    del K
+    if st["status"] != 0 or st["mark_iters"] < 0:
+        raise RuntimeError(f"oracle solve of {p.name} failed: {st}")
+    rec = {"assemble_s": t_asm, "element_loop_s": None, "solve_to_mark_s": st["mark_s"],
+           "iterations_to_mark": st["mark_iters"], "mark_rtol": mark, "iterations": st["iters"],
+           "relres": st["relres"], "solve_s": st["seconds"], "cpu_s": t_asm + st["mark_s"],
+           "threads": threads}
+    return u, rec
+
+
+def oracle_solution(p, threads):
+    """The oracle's displacement for a served or batched problem: C assembly,
+    then the elimination of examples/vector3D.jl:315-322 solved by a sparse
+    LU factorisation (2D; the same direct-solve family as the reference's
+    dense inverse) or Jacobi-PCG to 1e-13 (3D)."""
+    from oracle import coracle, fem_ref
+    coracle.build()
+    K = coracle.assemble(p.ne, p.NodeList, p.IEN, p.ndim, "Q1", p.ndim, p.ID, p.Young,
+                         p.nu if np.size(p.nu) > 1 else float(p.nu[0]), plane=p.plane, nthreads=threads)
+    if p.ndim == 2:
+        u = fem_ref.solve_eliminated(K.arrays(), p.fixed_dofs, p.fixed_vals, method="splu")
+        return u, "C assembly + sparse LU of K_free"
+    u, st = K.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13, nthreads=threads)
+    if st["status"] != 0:
+        raise RuntimeError(f"oracle solve of {p.name} failed: {st}")
+    return u, "C assembly + Jacobi-PCG to 1e-13"
+
+
+def _rel(u, ref):
+    return float(np.linalg.norm(np.asarray(u) - ref) / np.linalg.norm(ref))
+
+
 def _pcg_iteration_s(K, q, iters, threads):
     """Seconds per Jacobi-PCG iteration of the oracle on K: the difference of
-    a 1-iteration and an (iters + 1)-iteration solve, after a warm-up solve
-    (the first solve also pays for first-touch of its work arrays)."""
+    a 1-iteration and an (iters + 1)-iteration solve, after a warm-up solve."""
     K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=1, nthreads=threads)
     _, st1 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=1, nthreads=threads)
     _, st2 = K.solve(q.fixed_dofs, q.fixed_vals, rtol=0.0, max_iters=iters + 1, nthreads=threads)
@@ -235,38 +337,10 @@ def _pcg_iteration_s(K, q, iters, threads):
     return (st2["seconds"] - st1["seconds"]) / iters
 
 
-def cpu_sample(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=64, sample_iters=40):
-    """Time the oracle's assembly of the ``sample_ne``^3 instance of the same
-    generator (element loop + COO->CSC, scaled by the element-count ratio)
-    and ``sample_iters`` of its Jacobi-PCG iterations (scaled by the nnz ratio
-    and by ``iters_full``, the iteration count of the full-size solve).
-    Returns (DOF/s estimate for the full workload, details)."""
-    from oracle import coracle
-    coracle.build()
-    threads = _host_threads()
-    q = pkg.meshgen.jittered_cube(ne=sample_ne)
-    t0 = time.perf_counter()
-    K = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3, nthreads=threads)
-    t_asm = time.perf_counter() - t0
-    t_iter = _pcg_iteration_s(K, q, sample_iters, threads)
-    _, _, nzs, _, n_s = K.arrays()
-    nnz_s = len(nzs)
-    del K
-    scale_el = (ne_full / sample_ne) ** 3
-    t_full = t_asm * scale_el + t_iter * (nnz_full / nnz_s) * iters_full
-    return n_dof_full / t_full, {
-        "cores": threads, "t_assemble_sample_s": t_asm, "t_iter_sample_s": t_iter,
-        "est_full_s": t_full,
-        "sample": (f"oracle assembly (element loop + COO->CSC) of the {sample_ne}^3 instance of the same "
-                   f"generator scaled x{scale_el:.0f} by element count, plus {sample_iters} of its "
-                   f"Jacobi-PCG iterations scaled by nnz ({nnz_full}/{nnz_s}) and by the "
-                   f"{iters_full} iterations the full {ne_full}^3 solve takes")}
-
-
 def cpu_single_thread(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=32, sample_iters=20):
-    """The same estimate as cpu_sample with ONE thread (the reference's serial
-    element loop): the sample_ne^3 instance's assembly and sample_iters of
-    its Jacobi-PCG iterations, scaled to the full workload."""
+    """ESTIMATE of the oracle on ONE thread (the reference's serial element
+    loop): the sample_ne^3 instance's assembly and sample_iters of its
+    Jacobi-PCG iterations, scaled to the full workload."""
     from oracle import coracle
     q = pkg.meshgen.jittered_cube(ne=sample_ne)
     t0 = time.perf_counter()
@@ -277,17 +351,15 @@ def cpu_single_thread(pkg, ne_full, n_dof_full, nnz_full, iters_full, sample_ne=
     del K
     scale_el = (ne_full / sample_ne) ** 3
     t_full = t_asm * scale_el + t_iter * (nnz_full / nnz_s) * iters_full
-    return {"value": n_dof_full / t_full, "unit": UNIT, "cores": 1, "est_full_s": t_full,
+    return {"value": n_dof_full / t_full, "unit": UNIT, "cores": 1, "est_full_s": t_full, "kind": "estimate",
             "sample": (f"oracle on one thread: {sample_ne}^3 assembly scaled x{scale_el:.0f} by element count, "
                        f"plus {sample_iters} Jacobi-PCG iterations scaled by nnz and by {iters_full} iterations")}
 
 
 def dense_inverse_solve(pkg, sample_ne=10):
-    """The reference's own solve (examples/vector3D.jl:318,320: the dense
-    inverse of K_free) on the 20^3 parity problem, estimated from the
-    sample_ne^3 instance with the same boundary conditions: NumPy's LAPACK
-    inverse timed there and scaled by (n_free(20^3) / n_free(sample))^3."""
-    import os
+    """ESTIMATE of the reference's own solve (examples/vector3D.jl:318,320:
+    the dense inverse of K_free) on the 20^3 parity problem: NumPy's LAPACK
+    inverse timed on the sample_ne^3 instance, scaled by (n_free ratio)^3."""
     from oracle import coracle
     q = pkg.meshgen.hex_problem(sample_ne, 1001, jitter=0.0, top="sin", rtol=1e-12)
     full = pkg.meshgen.parity_cube20()
@@ -305,56 +377,93 @@ def dense_inverse_solve(pkg, sample_ne=10):
     nf_full = full.n_dof - len(full.fixed_dofs)
     threads = os.environ.get("OPENBLAS_NUM_THREADS") or os.environ.get("OMP_NUM_THREADS") or str(os.cpu_count())
     est = t * (nf_full / len(free)) ** 3
-    return {"problem": "20^3 parity cube (27,783 DOF, 26,019 free)", "est_s": est,
+    return {"problem": "20^3 parity cube (27,783 DOF, 26,019 free)", "est_s": est, "kind": "estimate",
             "dof_per_s": full.n_dof / est, "threads": int(threads),
             "sample": f"numpy.linalg.inv of the {len(free)}-DOF K_free of the {sample_ne}^3 instance: "
                       f"{t:.3f} s, scaled by (26019/{len(free)})^3"}
 
 
+def headline_config(args, world):
+    """The workload both arms report (identical dicts: same config)."""
+    ne = args.ne
+    nnz = 9 * (3 * (ne + 1) - 2) ** 3
+    return {"workload": f"{ne}^3 jittered Q1 hex elasticity, E ~ lognormal(0, 0.5), nu 0.3: FP64 assembly "
+                        f"+ Dirichlet elimination + Jacobi-PCG to {args.rtol:g}",
+            "ne": ne, "n_dof": 3 * (ne + 1) ** 3, "nnz": nnz, "precision": "fp64", "precond": "jacobi",
+            "rtol": args.rtol, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (K alone is %.1f GB), no flush" % (nnz * 8 / 1e9)}
+
+
+DATA = "synthetic: seeded jittered Q1 hex mesh, E ~ lognormal(0, 0.5), 4-mode top displacement"
+
+
 def reference_arm(args, dist):
-    """--impl reference: the reference's algorithm on the host cores (oracle port)."""
+    """--impl reference: the reference's algorithm (the C port) on the host
+    cores.  Warm-up steps are full runs of the 16^3 instance; the K timed
+    steps together are ONE full run of the stated workload: step 1 the
+    assembly (element loop + COO -> CSC), steps 2..K the Jacobi-PCG
+    iterations in equal chunks, the last one until the residual reaches the
+    stated tolerance.  value = DOFs / (sum of the K step times)."""
     if dist.rank != 0:
         return 0
-    pkg = GE.load_package()
-    ne = args.ne
-    n_dof = 3 * (ne + 1) ** 3
-    nnz = 9 * (3 * (ne + 1) - 2) ** 3
-    # Iteration count of the full-size Jacobi-PCG: from the full solve of the
-    # sample instance, scaled linearly in ne (Jacobi-PCG on Q1 elasticity:
-    # sqrt(cond) ~ 1/h).
     from oracle import coracle
     coracle.build()
-    sample_ne = min(64, ne)
-    q = pkg.meshgen.jittered_cube(ne=sample_ne)
-    Kq = coracle.assemble(q.ne, q.NodeList, q.IEN, 3, "Q1", 3, q.ID, q.Young, 0.3,
-                          nthreads=_host_threads())
-    _, st = Kq.solve(q.fixed_dofs, q.fixed_vals, rtol=args.rtol, nthreads=_host_threads())
-    del Kq
-    iters_full = int(round(st["iters"] * ne / sample_ne))
-    vals = []
-    for k in range(args.warmup + args.steps):
+    pkg = GE.load_package()
+    threads = _host_threads()
+    ne, K_steps = args.ne, max(1, args.steps)
+    cfg = headline_config(args, dist.world)
+    line = {"metric": METRIC, "impl": "reference", "unit": UNIT, "n_gpus": args.gpus, "steps": K_steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": DATA, "config": cfg}
+    ok, need, avail = _oracle_fits(ne ** 3)
+    if not ok:
+        print(json.dumps({"impl": "reference", "unavailable": f"the full {ne}^3 run needs ~{need:.0f} GB of "
+                          f"host memory, {avail:.0f} GB available"}), flush=True)
+        return 0
+    small = pkg.meshgen.jittered_cube(ne=16)
+    for _ in range(args.warmup):
+        Ks = coracle.assemble(small.ne, small.NodeList, small.IEN, 3, "Q1", 3, small.ID, small.Young, 0.3,
+                              nthreads=threads)
+        Ks.solve(small.fixed_dofs, small.fixed_vals, rtol=args.rtol, nthreads=threads)
+        del Ks
+    p = pkg.meshgen.jittered_cube(ne=ne)
+    est_iters = max(1, int(round(15.4 * ne)))   # Jacobi-PCG to 1e-10 on this family: ~1,970 at 128^3
+    chunk = math.ceil(est_iters / max(1, K_steps - 1))
+    times = []
+    t0 = time.perf_counter()
+    K = coracle.assemble(p.ne, p.NodeList, p.IEN, 3, "Q1", 3, p.ID, p.Young, 0.3, nthreads=threads)
+    t_asm = time.perf_counter() - t0
+    P = None
+    if K_steps == 1:
+        P = coracle.PcgSolve(K, p.fixed_dofs, p.fixed_vals, nthreads=threads)
+        P.run(10 ** 7, args.rtol)
+    times.append(time.perf_counter() - t0)
+    for k in range(1, K_steps):
         t0 = time.perf_counter()
-        v, det = cpu_sample(pkg, ne, n_dof, nnz, iters_full, sample_ne=sample_ne)
-        if k >= args.warmup:
-            vals.append((v, time.perf_counter() - t0, det))
-    value = float(np.median([v for v, _, _ in vals]))
-    det = vals[-1][2]
-    line = {
-        "metric": METRIC, "impl": "reference", "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": float(np.mean([t for _, t, _ in vals]) * 1e3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: seeded jittered Q1 hex mesh, E ~ lognormal(0, 0.5), 4-mode top displacement",
-        "config": {"workload": f"{ne}^3 Q1 hex elasticity, FP64 assembly + Jacobi-PCG to {args.rtol:g}",
-                   "ne": ne, "n_dof": n_dof, "nnz": nnz,
-                   "iterations_full_estimate": iters_full,
-                   "iterations_sample_full_solve": st["iters"]},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": det["cores"], "kind": "port",
-                         "sample": det["sample"],
-                         "single_thread": cpu_single_thread(pkg, ne, n_dof, nnz, iters_full),
-                         "reference_dense_solve": dense_inverse_solve(pkg)},
+        if P is None:
+            P = coracle.PcgSolve(K, p.fixed_dofs, p.fixed_vals, nthreads=threads)
+        P.run(10 ** 7 if k == K_steps - 1 else chunk, args.rtol)
+        times.append(time.perf_counter() - t0)
+    u, st = P.finish()
+    del K, P
+    if st["status"] != 0:
+        print(json.dumps({"impl": "reference", "unavailable": f"oracle solve did not converge: {st}"}), flush=True)
+        return 0
+    total = float(sum(times))
+    value = p.n_dof / total
+    line.update({
+        "value": value, "ms_per_step": total / K_steps * 1e3,
+        "iterations": st["iters"], "relres": st["relres"],
+        "breakdown_s": {"assemble": t_asm, "dirichlet_solve": total - t_asm},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": (f"the {K_steps} timed steps together are one full {ne}^3 run: step 1 the "
+                                    f"assembly (element loop on {threads} threads + serial COO -> CSC), steps "
+                                    f"2..{K_steps} the Jacobi-PCG iterations in chunks of {chunk}, the last to "
+                                    f"relres {args.rtol:g}; warm-up: {args.warmup} full runs of the 16^3 "
+                                    "instance")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+        "step_s": times,
+    })
     print(json.dumps(line), flush=True)
     return 0
 
@@ -362,6 +471,16 @@ def reference_arm(args, dist):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+
+def _device_problem(p, dev):
+    """Device copies of a problem's inputs in the reference's (column-major) order."""
+    import torch
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(np.asfortranarray(a).ravel(order="F"))).to(dev)  # noqa: E731
+    d = {"X": t(p.NodeList), "IEN": t(p.IEN), "ID": t(p.ID), "Y": torch.from_numpy(np.ascontiguousarray(p.Young)).to(dev),
+         "NU": torch.from_numpy(np.ascontiguousarray(p.nu, dtype=np.float64)).to(dev),
+         "FD": torch.from_numpy(p.fixed_dofs).to(dev), "FV": torch.from_numpy(p.fixed_vals).to(dev)}
+    return d
+
 
 def our_arm(args, dist):
     import torch
@@ -372,30 +491,38 @@ def our_arm(args, dist):
     dev = torch.device("cuda", dev_index)
     ctx = pkg.get_context(dev_index)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    threads = _host_threads()
+    one = dist.world == 1
 
     p = pkg.meshgen.jittered_cube(ne=args.ne)
     nN, nEl = p.n_nodes, p.n_elem
     n_dof = p.n_dof
-    NLf = np.asfortranarray(p.NodeList)
-    IENf = np.asfortranarray(p.IEN)
-    IDf = np.asfortranarray(p.ID)
-    # device-resident inputs in the reference's (column-major) memory order
-    dX = torch.from_numpy(NLf.ravel(order="F")).to(dev)
-    dIEN = torch.from_numpy(IENf.ravel(order="F")).to(dev)
-    dID = torch.from_numpy(IDf.ravel(order="F")).to(dev)
-    dY = torch.from_numpy(p.Young).to(dev)
-    dNU = torch.tensor([0.3], dtype=torch.float64, device=dev)
-    dFD = torch.from_numpy(p.fixed_dofs).to(dev)
-    dFV = torch.from_numpy(p.fixed_vals).to(dev)
+    line = {"metric": METRIC, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": DATA, "config": headline_config(args, dist.world)}
+
+    # ---- oracle: the reference's path on the host cores (N = 1 only) -------
+    uref_h, ref_name, oracle_rec = None, None, None
+    if "oracle" in args.legs and one:
+        ok, need, avail = _oracle_fits(nEl)
+        if ok:
+            uref_h, oracle_rec = oracle_full_run(p, threads, rtol=1e-13, mark=args.rtol)
+            ref_name = (f"oracle (C restatement of the reference, {threads} host threads): FP64 assembly + "
+                        f"Jacobi-PCG to relres 1e-13 ({oracle_rec['iterations']} iterations)")
+            line["oracle"] = oracle_rec
+        else:
+            line["oracle"] = {"skipped": f"needs ~{need:.0f} GB host memory, {avail:.0f} GB available"}
+
+    d = _device_problem(p, dev)
     dU = torch.empty(n_dof, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
 
     def step(precision="fp64", precond="jacobi", rtol=args.rtol, profile=False, out=dU, delta=0.1):
         t0 = time.perf_counter()
-        m = pkg.Mesh(p.ne, dX, dIEN, 3, "Q1", 3, dID, ctx=ctx, nNodes=nN, nen=8, ldIEN=nEl)
-        K = m.assemble(dY, dNU)
+        m = pkg.Mesh(p.ne, d["X"], d["IEN"], 3, "Q1", 3, d["ID"], ctx=ctx, nNodes=nN, nen=8, ldIEN=nEl)
+        K = m.assemble(d["Y"], d["NU"])
         t1 = time.perf_counter()
-        _, st = K.solve(dFD, dFV, precision=precision, precond=precond, rtol=rtol, profile=profile,
+        _, st = K.solve(d["FD"], d["FV"], precision=precision, precond=precond, rtol=rtol, profile=profile,
                         out=out, reliable_delta=delta)
         t2 = time.perf_counter()
         info = dict(st, n=K.n, nnz=K.nnz, asm_s=t1 - t0, solve_s=t2 - t1)
@@ -422,51 +549,47 @@ def our_arm(args, dist):
         dist.barrier()
         return ms, infos, ctx.kernel_launches() - launches0
 
-    # reference displacement for the error report: FP64 Jacobi-PCG to 1e-13 (untimed)
-    uref = torch.empty_like(dU)
-    ref_info = step(rtol=1e-13, out=uref)
-    uref_h = uref.cpu().numpy()
+    if uref_h is None:
+        # no oracle here (N > 1, or not enough host memory): a tight FP64 GPU solve, named as such
+        uref = torch.empty_like(dU)
+        step(rtol=1e-13, out=uref)
+        uref_h = uref.cpu().numpy()
+        ref_name = "FP64 Jacobi-PCG on the GPU to relres 1e-13 (the oracle did not run here)"
 
     def rel_err(u):
-        return float(np.linalg.norm(u.cpu().numpy() - uref_h) / np.linalg.norm(uref_h))
+        return _rel(u.cpu().numpy() if hasattr(u, "cpu") else u, uref_h)
 
-    # ---- value: FP64 path, device-resident inputs, SpMV launches event-timed
-    line = {"metric": METRIC, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64",
-            "data": "synthetic: seeded jittered Q1 hex mesh, E ~ lognormal(0, 0.5), 4-mode top displacement"}
-    it = ref_info["iterations"]
-    nnz = ref_info["nnz"]
+    nnz = 9 * (3 * (args.ne + 1) - 2) ** 3
+    hbm_peak, peak_kind = measured_peaks()
     if "value" in args.legs:
+        # ---- value: FP64 path as users run it (graph path), inputs in HBM
         clocks = ClockSampler(dev_index)
         clocks.start()
-        ms, infos, launches = timed(lambda: step(profile=True), args.steps, args.warmup)
+        ms, infos, launches = timed(lambda: step(), args.steps, args.warmup)
         clk = clocks.stop()
-        it = infos[-1]["iterations"]
         err64 = rel_err(dU)
         value, ms = aggregate(dist, n_dof, ms)
-        spmv_ms = sum(i["ms_spmv"] for i in infos) / max(1, sum(i["spmv_launches"] for i in infos))
+        # roofline of the dominant kernel: a separate profiled pass of the same step
+        prof = step(profile=True)
+        spmv_ms = prof["ms_spmv"] / max(1, prof["spmv_launches"])
         nnzb = nnz // 9
         nd = 3 * nN
         spmv_bytes = nnz * 8 + nnzb * 4 + nd * 8 * 2 + nd
-        hbm_peak, peak_kind = measured_peaks()
         achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
-        fp64_peak, fp32_peak = probe_fp64_peak(dev_index)
+        fp64_peak, fp32_peak, dmma_peak = probe_fp64_peak(dev_index)
         line.update({
             "value": value, "ms_per_step": ms,
-            "config": {"workload": f"{args.ne}^3 jittered Q1 hex elasticity, E ~ lognormal(0, 0.5): FP64 "
-                                   f"assembly + Jacobi-PCG to {args.rtol:g}",
-                       "ne": args.ne, "n_dof": n_dof, "nnz": nnz, "precision": "fp64", "precond": "jacobi",
-                       "rtol": args.rtol, "parallelism": f"replicas x{dist.world}",
-                       "l2": "inputs larger than L2 (K alone is %.1f GB), no flush" % (nnz * 8 / 1e9)},
-            "iterations": it, "relres": infos[-1]["relres"], "rel_err": err64,
-            "rel_err_reference": "FP64 Jacobi-PCG on the GPU to relative residual 1e-13",
+            "iterations": infos[-1]["iterations"], "relres": infos[-1]["relres"], "rel_err": err64,
+            "rel_err_reference": ref_name,
             "breakdown_s": {"upload_pattern_assemble": float(np.mean([i["asm_s"] for i in infos])),
                             "dirichlet_solve": float(np.mean([i["solve_s"] for i in infos]))},
             "roofline": {"kernel": "k_spmv<double,3> (masked sliced-ELL 3x3-block SpMV, fused p.Ap)",
                          "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": spmv_bytes, "launch_ms": spmv_ms,
+                         "timing": (f"CUDA events around each of the {prof['spmv_launches']} SpMV launches of a "
+                                    f"profiled pass of the same step ({prof['ms_total']:.0f} ms, kernels enqueued "
+                                    f"one by one; the timed steps run the graph path)"),
                          "traffic": SPMV64_TRAFFIC_PER_NNZ * nnz,
                          "traffic_source": "ncu capture at 64^3 scaled by stored entries"},
             "gpu_launches": int(launches),
@@ -475,46 +598,47 @@ def our_arm(args, dist):
         if fp64_peak:
             fl = 2.0 * nnz / (spmv_ms * 1e-3) / 1e12
             line["fp64_pipe"] = {"spmv_tflops": fl, "probe_fp64_tflops": fp64_peak, "frac": fl / fp64_peak,
-                                 "probe_fp32_tflops": fp32_peak}
+                                 "probe_fp32_tflops": fp32_peak, "probe_dmma_tflops": dmma_peak}
     if "mixed" in args.legs:
-        line["mixed"] = {}
+        line["mixed"] = {"rel_err_reference": ref_name}
     if "mixed" in args.legs and args.mixed_precond != "multigrid":
-        # ---- mixed precision on the same workload
-        msm, infm, _ = timed(lambda: step(precision="mixed", precond="block_jacobi", profile=True),
-                             args.steps, args.warmup)
+        msm, infm, _ = timed(lambda: step(precision="mixed", precond="block_jacobi"), args.leg_steps,
+                             args.leg_warmup)
+        err = rel_err(dU)
         vmix, msm = aggregate(dist, n_dof, msm)
-        spmv32_ms = sum(i["ms_spmv"] for i in infm) / max(1, sum(i["spmv_launches"] for i in infm))
+        prof = step(precision="mixed", precond="block_jacobi", profile=True)
+        spmv32_ms = prof["ms_spmv"] / max(1, prof["spmv_launches"])
         nnzb = nnz // 9
         up_blocks = (nnzb - nN) // 2 + nN
         lo_blocks = (nnzb - nN) // 2
         # per DOF: the old direction and z read, the new direction and y written
         # (the direction update runs inside this SpMV), the fixed flag
         sym_bytes = up_blocks * (36 + 4) + lo_blocks * 8 + 3 * nN * (4 * 4 + 1)
-        hbm_peak, peak_kind = measured_peaks()
-        line["mixed"] = {"value": vmix, "ms_per_step": msm,
-                         "precond": "block_jacobi", "iterations": infm[-1]["iterations"],
-                         "fp64_refreshes": infm[-1]["reliable_updates"], "relres": infm[-1]["relres"],
-                         "rel_err": rel_err(dU),
-                         "speedup_vs_fp64": (line["ms_per_step"] / msm) if "ms_per_step" in line else None,
-                         "spmv32": {"kernel": "k_spmv_sym<float,3> (upper-triangle 3x3 blocks, FP32)",
-                                    "launch_ms": spmv32_ms, "algorithmic_bytes_per_launch": sym_bytes,
-                                    "achieved_gbs": sym_bytes / (spmv32_ms * 1e-3) / 1e9,
-                                    "frac_hbm": sym_bytes / (spmv32_ms * 1e-3) / 1e9 / hbm_peak}}
+        line["mixed"].update({
+            "value": vmix, "ms_per_step": msm, "steps": args.leg_steps, "precond": "block_jacobi",
+            "iterations": infm[-1]["iterations"], "fp64_refreshes": infm[-1]["reliable_updates"],
+            "relres": infm[-1]["relres"], "rel_err": err,
+            "speedup_vs_fp64": (line["ms_per_step"] / msm) if "ms_per_step" in line else None,
+            "spmv32": {"kernel": "k_spmv_sym<float,3> (upper-triangle 3x3 blocks, FP32, direction update fused)",
+                       "launch_ms": spmv32_ms, "algorithmic_bytes_per_launch": sym_bytes,
+                       "achieved_gbs": sym_bytes / (spmv32_ms * 1e-3) / 1e9,
+                       "frac_hbm": sym_bytes / (spmv32_ms * 1e-3) / 1e9 / hbm_peak,
+                       "timing": "CUDA events around each SpMV of a profiled pass of the same step"}})
     if "mixed" in args.legs and args.mixed_precond != "block_jacobi":
-        # the same mixed solve with the geometric multigrid preconditioner (structured mesh)
         msg, infg, _ = timed(lambda: step(precision="mixed", precond="multigrid", delta=args.mg_delta),
-                             args.steps, args.warmup)
+                             args.leg_steps, args.leg_warmup)
+        err = rel_err(dU)
         vmg, msg = aggregate(dist, n_dof, msg)
         line["mixed"]["multigrid"] = {
-            "value": vmg, "ms_per_step": msg, "iterations": infg[-1]["iterations"],
-            "fp64_refreshes": infg[-1]["reliable_updates"], "relres": infg[-1]["relres"], "rel_err": rel_err(dU),
+            "value": vmg, "ms_per_step": msg, "steps": args.leg_steps, "iterations": infg[-1]["iterations"],
+            "fp64_refreshes": infg[-1]["reliable_updates"], "relres": infg[-1]["relres"], "rel_err": err,
             "speedup_vs_fp64": (line["ms_per_step"] / msg) if "ms_per_step" in line else None,
             "assemble_s": infg[-1]["asm_s"], "solve_s": infg[-1]["solve_s"], "reliable_delta": args.mg_delta}
     if "e2e" in args.legs:
         # ---- e2e: C ABI with pinned host buffers, copies inside the timed region
         def pinned(a):
-            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-            return t.numpy()
+            return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+        NLf, IENf, IDf = (np.asfortranarray(a) for a in (p.NodeList, p.IEN, p.ID))
         hX = pinned(NLf.ravel(order="F")).reshape(NLf.shape, order="F")
         hIEN = pinned(IENf.ravel(order="F")).reshape(IENf.shape, order="F")
         hID = pinned(IDf.ravel(order="F")).reshape(IDf.shape, order="F")
@@ -530,90 +654,124 @@ def our_arm(args, dist):
         h2d = hX.nbytes + hIEN.nbytes + hID.nbytes + hY.nbytes + 8 + hFD.nbytes + hFV.nbytes
         line["e2e"] = {"value": ve2e, "unit": UNIT, "ms_per_step": mse,
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hU.nbytes),
-                       "rel_err": float(np.linalg.norm(hU - uref_h) / np.linalg.norm(uref_h))}
+                       "rel_err": _rel(hU, uref_h), "rel_err_reference": ref_name}
+    del d
+    torch.cuda.empty_cache()
     if "precision" in args.legs:
-        line["precision"] = precision_leg(args, pkg, ctx, stream, dist)
+        line["precision"] = precision_leg(args, pkg, ctx, stream, dist, threads)
     if "batch" in args.legs:
-        line["batch"] = batch_leg(args, pkg, ctx, stream, dist)
+        line["batch"] = batch_leg(args, pkg, ctx, stream, dist, threads)
     if "serve" in args.legs:
-        line["serve"] = serve_leg(args, pkg, ctx, dist)
-    if "cpu" in args.legs and dist.world == 1:
-        # ---- CPU baseline (rank 0, N=1 only)
-        v, det = cpu_sample(pkg, args.ne, n_dof, nnz, it)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",
-                                "sample": det["sample"],
-                                "single_thread": cpu_single_thread(pkg, args.ne, n_dof, nnz, it),
-                                "reference_dense_solve": dense_inverse_solve(pkg)}
+        line["serve"] = serve_leg(args, pkg, ctx, dist, threads)
+    if "cpu" in args.legs and one:
+        it = line.get("iterations") or 1971
+        cb = {"unit": UNIT, "kind": "port", "cores": threads}
+        if oracle_rec:
+            cb.update({"value": n_dof / oracle_rec["cpu_s"],
+                       "sample": (f"full {args.ne}^3 run of the oracle on {threads} host threads: assembly "
+                                  f"(element loop + serial COO -> CSC) {oracle_rec['assemble_s']:.1f} s + Dirichlet "
+                                  f"lift and Jacobi-PCG to relres {args.rtol:g} "
+                                  f"{oracle_rec['solve_to_mark_s']:.1f} s ({oracle_rec['iterations_to_mark']} "
+                                  "iterations); measured, not extrapolated")})
+        else:
+            cb.update({"value": None, "sample": line.get("oracle", {}).get("skipped", "oracle leg not run")})
+        cb["single_thread"] = cpu_single_thread(pkg, args.ne, n_dof, nnz, it)
+        cb["reference_dense_solve"] = dense_inverse_solve(pkg)
+        line["cpu_baseline"] = cb
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
-def precision_leg(args, pkg, ctx, stream, dist):
+def _timed_events(stream, fn, steps, warmup, dist):
+    import torch
+    for _ in range(warmup):
+        fn()
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    out = [fn() for _ in range(steps)]
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps, out
+
+
+def precision_leg(args, pkg, ctx, stream, dist, threads):
     """Precision workload: 96^3 jittered hex mesh, per-element E ~ lognormal(0, 1)
     (stiffness contrast ~1e3), nu ~ U(0.25, 0.45) per element, 4-mode top
     displacement.  Plain FP64 Jacobi-PCG against FP32-inner block-Jacobi PCG
-    with FP64 residual refreshes, both to 1e-10 relative residual; the mixed
-    result's error is measured against a tight FP64 solve (1e-13)."""
+    with FP64 residual refreshes (the stated method) and against the same
+    with multigrid, all to 1e-10 relative residual; errors against the
+    oracle's solution of the same problem (FP64 assembly and Jacobi-PCG to
+    1e-13 on the host), whose time to 1e-10 is reported too."""
     import torch
     p = pkg.meshgen.contrast_cube(ne=args.precision_ne)
     dev = torch.device("cuda", ctx.device)
-    NLf, IENf, IDf = (np.asfortranarray(a) for a in (p.NodeList, p.IEN, p.ID))
-    dX = torch.from_numpy(NLf.ravel(order="F")).to(dev)
-    dIEN = torch.from_numpy(IENf.ravel(order="F")).to(dev)
-    dID = torch.from_numpy(IDf.ravel(order="F")).to(dev)
-    dY = torch.from_numpy(p.Young).to(dev)
-    dNU = torch.from_numpy(np.ascontiguousarray(p.nu)).to(dev)
-    dFD = torch.from_numpy(p.fixed_dofs).to(dev)
-    dFV = torch.from_numpy(p.fixed_vals).to(dev)
+    uref_h, ref_name, orec = None, None, None
+    if "oracle" in args.legs and dist.world == 1 and _oracle_fits(p.n_elem)[0]:
+        uref_h, orec = oracle_full_run(p, threads, rtol=1e-13, mark=1e-10)
+        ref_name = (f"oracle (C restatement, {threads} host threads): FP64 assembly + Jacobi-PCG to relres 1e-13 "
+                    f"({orec['iterations']} iterations)")
+    d = _device_problem(p, dev)
     nN, nEl = p.n_nodes, p.n_elem
     dU = torch.empty(p.n_dof, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
 
-    def step(precision, precond, rtol, out=dU):
-        m = pkg.Mesh(p.ne, dX, dIEN, 3, "Q1", 3, dID, ctx=ctx, nNodes=nN, nen=8, ldIEN=nEl)
-        K = m.assemble(dY, dNU)
-        _, st = K.solve(dFD, dFV, precision=precision, precond=precond, rtol=rtol, out=out)
+    def step(precision, precond, rtol, out=dU, delta=0.1):
+        m = pkg.Mesh(p.ne, d["X"], d["IEN"], 3, "Q1", 3, d["ID"], ctx=ctx, nNodes=nN, nen=8, ldIEN=nEl)
+        K = m.assemble(d["Y"], d["NU"])
+        _, st = K.solve(d["FD"], d["FV"], precision=precision, precond=precond, rtol=rtol, out=out,
+                        reliable_delta=delta)
         K.close()
         m.close()
         return st
 
-    uref = torch.empty_like(dU)
-    step("fp64", "jacobi", 1e-13, out=uref)
-    uref_h = uref.cpu().numpy()
+    if uref_h is None:
+        uref = torch.empty_like(dU)
+        step("fp64", "jacobi", 1e-13, out=uref)
+        uref_h = uref.cpu().numpy()
+        ref_name = "FP64 Jacobi-PCG on the GPU to relres 1e-13 (the oracle did not run here)"
 
-    def run(precision, precond):
-        for _ in range(args.warmup):
-            step(precision, precond, 1e-10)
-        dist.barrier()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        sts = [step(precision, precond, 1e-10) for _ in range(args.steps)]
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
-        err = float(np.linalg.norm(dU.cpu().numpy() - uref_h) / np.linalg.norm(uref_h))
+    def run(precision, precond, delta=0.1):
+        ms, sts = _timed_events(stream, lambda: step(precision, precond, 1e-10, delta=delta), args.leg_steps,
+                                args.leg_warmup, dist)
+        err = _rel(dU.cpu().numpy(), uref_h)
         v, ms = aggregate(dist, p.n_dof, ms)
-        return {"value": v, "unit": UNIT, "ms_per_step": ms, "iterations": sts[-1]["iterations"],
-                "fp64_refreshes": sts[-1]["reliable_updates"], "relres": sts[-1]["relres"], "rel_err": err}
+        return {"value": v, "unit": UNIT, "ms_per_step": ms, "steps": args.leg_steps,
+                "iterations": sts[-1]["iterations"], "fp64_refreshes": sts[-1]["reliable_updates"],
+                "relres": sts[-1]["relres"], "rel_err": err}
 
     fp64 = run("fp64", "jacobi")
     mixed = run("mixed", "block_jacobi")
-    return {"workload": f"{p.ne}^3 Q1 hex elasticity, E ~ lognormal(0, 1), nu ~ U(0.25, 0.45) per element; "
-                        "assemble + Dirichlet + PCG to 1e-10, inputs on the device",
-            "n_dof": p.n_dof, "fp64_jacobi": fp64, "mixed_block_jacobi": mixed,
-            "speedup_mixed_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
-            "rel_err_reference": "FP64 Jacobi-PCG on the GPU to relative residual 1e-13"}
+    mg = run("mixed", "multigrid", args.mg_delta)
+    del d
+    out = {"workload": f"{p.ne}^3 Q1 hex elasticity, E ~ lognormal(0, 1), nu ~ U(0.25, 0.45) per element; "
+                       "assemble + Dirichlet + PCG to 1e-10, inputs on the device",
+           "n_dof": p.n_dof, "fp64_jacobi": fp64, "mixed_block_jacobi": mixed, "mixed_multigrid": mg,
+           "speedup_mixed_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
+           "speedup_mixed_multigrid_vs_fp64": fp64["ms_per_step"] / mg["ms_per_step"],
+           "rel_err_reference": ref_name}
+    if orec:
+        out["oracle"] = dict(orec, cpu_dof_per_s=p.n_dof / orec["cpu_s"])
+    return out
 
 
-def batch_leg(args, pkg, ctx, stream, dist):
+def _batch_arm(name):
+    precision, precond = name.split("_", 1)
+    return precision, precond
+
+
+def batch_leg(args, pkg, ctx, stream, dist, threads):
     """Batching workload: ``batch_count`` plane-strain unit squares, n ~ U{16..256},
     jitter 0.15h, E = 1, nu_mesh ~ U(0.2, 0.45), clamped left edge, 3-mode right
-    edge u_x; mixed-precision block-Jacobi PCG to 1e-8 in one persistent launch.
-    Beside it: the plain FP64 GPU path (single-mesh API, Jacobi-PCG, one mesh
-    after another) on the same meshes."""
-    import torch
+    edge u_x, in one persistent launch per solve.  Every arm solves the same
+    batch with the same machinery and accounting (set-up excluded from all):
+    FP64 block Jacobi, mixed block Jacobi and mixed multigrid, each with its
+    own autotuned launch shape.  Precision factor = FP64 / mixed (block
+    Jacobi both), preconditioner factor = block Jacobi / multigrid (mixed
+    both).  Errors against the oracle's sparse-direct solution of every k-th
+    mesh."""
     probs = pkg.meshgen.quad_batch(count=args.batch_count)
     n_total = int(sum(p.n_dof for p in probs))
     nus = np.array([float(p.nu[0]) for p in probs])
@@ -625,72 +783,67 @@ def batch_leg(args, pkg, ctx, stream, dist):
     # the workload states PCG to 1e-8; the metric needs 1e-8 error in u, which
     # this stiff plane-strain family reaches at a 1e-12 relative residual
     rtol = args.batch_rtol
-    delta = args.mg_delta if args.batch_precond == "multigrid" else 0.1
-    t0 = time.perf_counter()
-    # tuning trials: full solves of a quarter of the meshes, taken evenly
-    # from the size order (capping iterations would hide what clusters buy on
-    # the largest meshes)
-    if args.batch_launch:
-        bt.set_launch(*[int(x) for x in args.batch_launch.split(",")])
-        shape, tuned_ms = bt.launch(), None
-    else:
-        shape, tuned_ms = bt.autotune(1.0, nus, fixed, vals, plane="strain", precision="mixed",
-                                      precond=args.batch_precond, rtol=rtol, sample=max(1, len(probs) // 4),
-                                      reliable_delta=delta)
-    t_tune = time.perf_counter() - t0
+    k_s = max(1, len(probs) // max(1, args.oracle_samples))
+    sample = list(range(0, len(probs), k_s))
+    refs = {}
+    if "oracle" in args.legs and dist.world == 1:
+        for k in sample:
+            refs[k], how = oracle_solution(probs[k], threads)
+        ref_name = f"oracle on every {k_s}th mesh ({len(sample)} meshes): {how}"
+    arms = {}
+    try:
+        for name in [a.strip() for a in args.batch_arms.split(",") if a.strip()]:
+            precision, precond = _batch_arm(name)
+            delta = args.mg_delta if precond == "multigrid" else 0.1
+            kw = dict(plane="strain", precision=precision, precond=precond, rtol=rtol, reliable_delta=delta)
+            t0 = time.perf_counter()
+            if args.batch_launch:
+                bt.set_launch(*[int(x) for x in args.batch_launch.split(",")])
+                shape = bt.launch()
+            else:  # full solves of an eighth of the meshes, taken evenly from the size order
+                shape, _ = bt.autotune(1.0, nus, fixed, vals, sample=max(1, len(probs) // 8), **kw)
+            t_tune = time.perf_counter() - t0
+            ms, outs = _timed_events(stream, lambda: bt.solve(1.0, nus, fixed, vals, **kw),
+                                     args.leg_steps, min(args.leg_warmup, 1), dist)
+            value, ms = aggregate(dist, n_total, ms)
+            u, st = outs[-1]
+            parts = bt.split(u)
+            its = np.array([s["iterations"] for s in st])
+            arm = {"value": value, "unit": UNIT, "ms_per_batch": ms, "steps": args.leg_steps,
+                   "autotune_s": t_tune, "launch": shape,
+                   "statuses_ok": int(sum(s["status"] == 0 for s in st)),
+                   "iterations": {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())},
+                   "mesh_ms": {"median": float(np.median([s["ms"] for s in st])),
+                               "max": float(max(s["ms"] for s in st))}}
+            if refs:
+                arm["rel_err_max_sample"] = max(_rel(parts[k], refs[k]) for k in sample)
+            arms[name] = arm
+    finally:
+        bt.close()
+    out = {"workload": f"{len(probs)} plane-strain Q1 quad meshes, n ~ U{{16..256}}, PCG to {rtol:g}, one "
+                       "persistent launch per solve",
+           "n_dof_total": n_total, "setup_s": t_setup,
+           "setup_note": "pattern build + upload of the batch, once, excluded from every arm",
+           "arms": arms}
+    if refs:
+        out["rel_err_reference"] = ref_name
+    f64, mbj, mmg = (arms.get(k) for k in ("fp64_block_jacobi", "mixed_block_jacobi", "mixed_multigrid"))
+    if mmg:
+        out.update({"value": mmg["value"], "unit": UNIT, "precond": "multigrid", "precision": "mixed"})
+    factors = {}
+    if f64 and mbj:
+        factors["precision"] = f64["ms_per_batch"] / mbj["ms_per_batch"]
+    if mbj and mmg:
+        factors["preconditioner"] = mbj["ms_per_batch"] / mmg["ms_per_batch"]
+    if f64 and mmg:
+        factors["both"] = f64["ms_per_batch"] / mmg["ms_per_batch"]
+    out["speedup_factors"] = dict(factors, basis="ms per batch, same meshes, same kernel, set-up excluded")
+    return out
 
-    def run_batch():
-        return bt.solve(1.0, nus, fixed, vals, plane="strain", precision="mixed",
-                        precond=args.batch_precond, rtol=rtol, reliable_delta=delta)
 
-    for _ in range(args.warmup):
-        u, st = run_batch()
-    dist.barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        u, st = run_batch()
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    value, ms = aggregate(dist, n_total, ms)
-    parts = bt.split(u)
-    # plain FP64 GPU path, one mesh after another, same stopping rule
-    t0 = time.perf_counter()
-    plain_u = []
-    for p in probs:
-        K = pkg.assemble_system(p.ne, p.NodeList, p.IEN, 2, "Q1", 2, p.ID, 1.0, float(p.nu[0]),
-                                plane="strain", ctx=ctx, as_handle=True)
-        plain_u.append(K.solve(p.fixed_dofs, p.fixed_vals, rtol=rtol)[0])
-        K.close()
-    t_plain = time.perf_counter() - t0
-    # error against tight FP64 solves on a sample of meshes
-    errs = []
-    for k in range(0, len(probs), max(1, len(probs) // 32)):
-        p = probs[k]
-        K = pkg.assemble_system(p.ne, p.NodeList, p.IEN, 2, "Q1", 2, p.ID, 1.0, float(p.nu[0]),
-                                plane="strain", ctx=ctx, as_handle=True)
-        ref = K.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13)[0]
-        K.close()
-        errs.append(float(np.linalg.norm(parts[k] - ref) / np.linalg.norm(ref)))
-    bt.close()
-    its = np.array([s["iterations"] for s in st])
-    pc = "geometric-multigrid" if args.batch_precond == "multigrid" else "block-Jacobi"
-    return {"workload": f"{len(probs)} plane-strain Q1 quad meshes, n ~ U{{16..256}}, mixed "
-                        f"{pc} PCG to {rtol:g}, one persistent launch",
-            "precond": args.batch_precond,
-            "n_dof_total": n_total, "value": value, "unit": UNIT, "ms_per_batch": ms,
-            "setup_s": t_setup, "autotune_s": t_tune, "launch": shape,
-            "statuses_ok": int(sum(s["status"] == 0 for s in st)),
-            "mesh_ms": {"median": float(np.median([s["ms"] for s in st])),
-                        "max": float(max(s["ms"] for s in st))},
-            "iterations": {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())},
-            "rel_err_max_sample": max(errs), "rel_err_reference": "FP64 PCG to 1e-13 on every "
-            f"{max(1, len(probs) // 32)}th mesh",
-            "plain_fp64_gpu": {"value": n_total / t_plain, "s": t_plain,
-                               "path": "single-mesh API per mesh: assemble + FP64 Jacobi-PCG"},
-            "speedup_vs_plain_fp64": (n_total / (ms * 1e-3)) / (n_total / t_plain)}
-
+# ---------------------------------------------------------------------------
+# serving
+# ---------------------------------------------------------------------------
 
 def _stream(srv_all, pool, arrivals, which):
     """Open-loop driver: a thread submits pool[which[i]] at arrivals[i] (s);
@@ -788,98 +941,175 @@ def _concurrency(recs):
     return float(sum(b - a for a, b in iv) / span) if span > 0 else 0.0
 
 
-def serve_leg(args, pkg, ctx, dist):
-    """Serving workload: an open-loop Poisson stream, 70% plane-strain quads
+def _submit_args(p):
+    return dict(topology_key=p.ndim * 100000 + p.ne, ndim=p.ndim, nDof=p.ndim, plane=p.plane)
+
+
+def _serve_closed(srv, probs):
+    """Submit every problem at once; returns (results, wall seconds)."""
+    t0 = time.perf_counter()
+    ids = [srv.submit(p.NodeList, p.IEN[: p.n_elem], p.ID, p.Young, p.nu, p.fixed_dofs, p.fixed_vals,
+                      **_submit_args(p)) for p in probs]
+    outs = [srv.wait(i, timeout_ms=600000) for i in ids]
+    return outs, time.perf_counter() - t0
+
+
+def _lat(a):
+    a = np.asarray(a, dtype=np.float64)
+    if a.size == 0:
+        return None
+    return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)), "max": float(a.max()),
+            "n": int(a.size)}
+
+
+def serve_leg(args, pkg, ctx, dist, threads):
+    """Serving workload: an open-loop Poisson stream of requests drawn fresh
+    from the serving distribution (no pool): 70% plane-strain quads
     n ~ U{32..512}, 30% hexes n ~ U{16..64}, per-element E ~ lognormal(0, 0.5),
-    nu ~ U(0.25, 0.45) per request, seeded boundary displacements; one server
-    (one persistent kernel for both element classes), topology key = class and
-    mesh size, mixed-precision block-Jacobi PCG.  Requests draw from a pool
-    of distinct meshes, so a repeated request must give the same bits."""
-    rng = np.random.default_rng(2005)
-    pool = [p for _, p in pkg.meshgen.serving_stream(args.serve_pool)]
-    rtol = args.batch_rtol
-    # the whole GPU for the kernel: after the warm-up every topology is cached, so
-    # no pattern build needs free SMs during the measured streams
-    # 8-CTA clusters of 256 threads (two per SM): measured 5% above 4 x 512 on this stream
+    nu ~ U(0.25, 0.45) per request, seeded boundary displacements.  One server
+    (one persistent kernel for both element classes), topology key = class
+    and mesh size (its pattern and hierarchy layout are cached; a request of
+    a new size builds its pattern when it is admitted), mixed-precision PCG
+    with the multigrid preconditioner.  Measured: the configured rate (the
+    backlog it builds is stated), a stream at half the measured capacity
+    (steady state), the cold-topology share of both, the same request set on
+    FP64 and mixed servers (precision and preconditioner factors), a pooled
+    bitwise-repeat check, and the error of sampled requests against the
+    oracle."""
     cl, th = (int(v) for v in args.serve_launch.split(","))
-    srv = pkg.Server(precision="mixed", precond=args.serve_precond, rtol=rtol, cluster=cl, threads=th,
-                     reliable_delta=args.mg_delta if args.serve_precond == "multigrid" else 0.1,
-                     sm_fraction=1.0, idle_exit_ms=200.0)
+    rtol = args.batch_rtol
+    nmain = args.serve_requests
+    main = list(pkg.meshgen.serving_stream(nmain, seed=2005, rate=args.serve_rate))
+    arrivals = np.array([t for t, _ in main])
+    probs = [p for _, p in main]
+    warm = [p for _, p in pkg.meshgen.serving_stream(8, seed=2004)]
+
+    def server(precision="mixed", precond="multigrid"):
+        return pkg.Server(precision=precision, precond=precond, rtol=rtol, cluster=cl, threads=th,
+                          reliable_delta=args.mg_delta if precond == "multigrid" else 0.1, idle_exit_ms=200.0)
+
+    out = {"workload": (f"open-loop Poisson stream, requests drawn fresh (no pool): 70% plane-strain quads "
+                        f"n ~ U{{32..512}}, 30% hexes n ~ U{{16..64}}, E ~ lognormal(0, 0.5), nu ~ U(0.25, 0.45); "
+                        f"mixed-precision PCG to {rtol:g} with geometric multigrid V(1,1); topology key = "
+                        "(class, n)"),
+           "launch": {"cluster": cl, "threads": th}, "unit": "requests/s"}
+    srv = server()
     try:
-        # warm-up: every pool mesh once (builds and caches each topology's pattern)
-        recs, t_warm = _stream(srv, pool, np.zeros(len(pool)), np.arange(len(pool)))
-        first = {k: u for k, u, _ in recs}
-        # saturation: the offered rate far above capacity
-        n = args.serve_requests
-        arr = np.cumsum(rng.exponential(1.0 / args.serve_rate, n))
-        which = rng.integers(0, len(pool), n)
-        recs, wall = _stream(srv, pool, arr, which)
+        _serve_closed(srv, warm)               # start-up: library, kernel, a few topologies
+        seen = {p.ndim * 100000 + p.ne for p in warm}
+        cold_main = []
+        for p in probs:
+            k = p.ndim * 100000 + p.ne
+            cold_main.append(k not in seen)
+            seen.add(k)
+        recs, wall = _stream(srv, probs, arrivals, np.arange(nmain))
         lat = np.array([r["total_ms"] for _, _, r in recs])
         gpu = np.array([r["gpu_ms"] for _, _, r in recs])
+        cold = np.array(cold_main)
         dofs = float(sum(r["ndof"] for _, _, r in recs))
-        same = sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs)
-        capacity = n / wall
-        sus_rps, sus_dps = _sustained(recs, lambda k: pool[k].n_dof)
-        traffic = _window_traffic(recs, pool, args.serve_precond == "multigrid")
-        peak = srv.info()
-        # below capacity: latency without a backlog
-        m = max(20, min(120, int(capacity * 8)))
-        rate = 0.5 * capacity
-        arr2 = np.cumsum(rng.exponential(1.0 / rate, m))
-        which2 = rng.integers(0, len(pool), m)
-        recs2, wall2 = _stream(srv, pool, arr2, which2)
+        capacity = nmain / wall
+        sus_rps, sus_dps = _sustained(recs, lambda k: probs[k].n_dof)
+        traffic = _window_traffic(recs, probs, True)
+        backlog = _backlog(arrivals, recs)
+        # steady state: half the measured capacity, fresh requests again
+        rate2 = 0.5 * capacity
+        m2 = max(40, min(240, int(capacity * 8)))
+        below = list(pkg.meshgen.serving_stream(m2, seed=2006, rate=rate2))
+        arr2 = np.array([t for t, _ in below])
+        probs2 = [p for _, p in below]
+        cold2 = []
+        for p in probs2:
+            k = p.ndim * 100000 + p.ne
+            cold2.append(k not in seen)
+            seen.add(k)
+        recs2, wall2 = _stream(srv, probs2, arr2, np.arange(m2))
         lat2 = np.array([r["total_ms"] for _, _, r in recs2])
-        same += sum(bool(np.array_equal(u, first[k])) for k, u, _ in recs2)
-        statuses_ok = sum(r["status"] == 0 for _, _, r in recs + recs2)
+        cold2 = np.array(cold2)
         info = srv.info()
+        statuses_ok = sum(r["status"] == 0 for _, _, r in recs + recs2)
+        u_main = {k: u for k, u, _ in recs}
     finally:
         srv.close()
-    # error against tight FP64 solves, and the plain FP64 GPU path, on a sample of the pool
-    sample = list(range(0, len(pool), max(1, len(pool) // 16)))
-    errs, t_plain, dof_plain = [], 0.0, 0
-    for k in sample:
-        p = pool[k]
-        t0 = time.perf_counter()   # the plain path per request: assemble + FP64 Jacobi-PCG
-        K = pkg.assemble_system(p.ne, p.NodeList, p.IEN, p.ndim, "Q1", p.ndim, p.ID, p.Young,
-                                float(p.nu[0]), plane=p.plane, ctx=ctx, as_handle=True)
-        K.solve(p.fixed_dofs, p.fixed_vals, rtol=rtol)
-        t_plain += time.perf_counter() - t0
-        ref = K.solve(p.fixed_dofs, p.fixed_vals, rtol=1e-13)[0]
-        K.close()
-        dof_plain += p.n_dof
-        errs.append(float(np.linalg.norm(first[k] - ref) / np.linalg.norm(ref)))
-    pct = lambda a, q: float(np.percentile(a, q))  # noqa: E731
-    return {"workload": f"open-loop Poisson stream at {args.serve_rate:g} req/s, {n} requests "
-                        f"from a pool of {len(pool)} meshes (70% quads n~U{{32..512}}, 30% hexes "
-                        f"n~U{{16..64}}), mixed-precision PCG to {rtol:g}, "
-                        + ("geometric multigrid V(1,1) cached per topology" if args.serve_precond == "multigrid"
-                           else "block Jacobi"),
-            "precond": args.serve_precond, "launch": {"cluster": cl, "threads": th},
-            "solves_per_s": capacity, "dof_per_s": dofs / wall, "unit": "requests/s",
-            "sustained": {"solves_per_s": sus_rps, "dof_per_s": sus_dps,
-                          "window": "first to last claim of the stream (device clock): requests always "
-                                    "waiting, every group busy"},
-            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max())},
-            "gpu_ms": {"p50": pct(gpu, 50), "p99": pct(gpu, 99)},
-            "below_capacity": {"rate": rate, "requests": m, "solves_per_s": m / wall2,
-                               "latency_ms": {"p50": pct(lat2, 50), "p99": pct(lat2, 99)}},
-            "repeat_bitwise_identical": f"{same}/{n + m}", "statuses_ok": int(statuses_ok),
-            "warmup_s": t_warm, "peak_inflight": peak["peak_inflight"], "peak_bytes": info["peak_bytes"],
-            "kernel_launches": info["kernel_launches"], "grid_ctas": info["grid"], "cluster": info["cluster"],
-            "gpu_concurrency": _concurrency(recs),
-            "cg_memory": None if traffic is None else {
-                "achieved_gbs": traffic["gbs"], "frac_hbm": traffic["gbs"] / measured_peaks()[0],
-                "basis": "iterations x (K blocks + column indices + 11 FP32 vectors per DOF, and with "
-                         "multigrid the V(1,1) cycle's two fine products and vectors plus coarse levels) of "
-                         "the requests finished in the saturated window, over that window; set-up not counted",
-                "group_time_share": traffic["group_time_share"],
-                "iterations_median": traffic["iterations_median"]},
-            "rel_err_max_sample": max(errs),
-            "plain_fp64_gpu": {"dof_per_s": dof_plain / t_plain,
-                               "path": "single-mesh API per request: assemble + FP64 Jacobi-PCG, "
-                                       "requests one after another"},
-            "speedup_vs_plain_fp64": (dofs / wall) / (dof_plain / t_plain),
-            "speedup_sustained_vs_plain_fp64": (sus_dps / (dof_plain / t_plain)) if sus_dps else None}
+    out.update({
+        "solves_per_s": capacity, "dof_per_s": dofs / wall,
+        "configured_rate": {"offered_per_s": args.serve_rate, "requests": nmain, "wall_s": wall,
+                            "latency_ms": _lat(lat), "gpu_ms": _lat(gpu),
+                            "max_backlog": backlog,
+                            "note": ("offered rate above capacity: the queue grows for the whole stream, so "
+                                     "latency here is set by the stream length (max_backlog requests waiting)")},
+        "steady_state": {"offered_per_s": rate2, "requests": m2, "solves_per_s": m2 / wall2,
+                         "latency_ms": _lat(lat2), "latency_ms_warm_topology": _lat(lat2[~cold2]),
+                         "latency_ms_cold_topology": _lat(lat2[cold2])},
+        "cache_hit_rate": float(1.0 - cold.mean()),
+        "cold_topology": {"requests": int(cold.sum()), "latency_ms": _lat(lat[cold]),
+                          "gpu_ms": _lat(gpu[cold])},
+        "warm_topology": {"latency_ms": _lat(lat[~cold]), "gpu_ms": _lat(gpu[~cold])},
+        "sustained": {"solves_per_s": sus_rps, "dof_per_s": sus_dps,
+                      "window": "first to last claim of the stream (device clock): requests always waiting"},
+        "statuses_ok": int(statuses_ok), "requests_total": nmain + m2,
+        "peak_inflight": info["peak_inflight"], "peak_bytes": info["peak_bytes"],
+        "kernel_launches": info["kernel_launches"], "grid_ctas": info["grid"],
+        "gpu_concurrency": _concurrency(recs),
+        "cg_memory": None if traffic is None else {
+            "achieved_gbs": traffic["gbs"], "frac_hbm": traffic["gbs"] / measured_peaks()[0],
+            "basis": "iterations x (K blocks + column indices + the CG vectors per DOF, the V(1,1) cycle's two "
+                     "fine products and vectors plus coarse levels) of the requests finished in the saturated "
+                     "window, over that window; set-up not counted",
+            "group_time_share": traffic["group_time_share"],
+            "iterations_median": traffic["iterations_median"]},
+    })
+    # errors against the oracle on sampled requests of the configured-rate stream
+    if "oracle" in args.legs and dist.world == 1:
+        k_s = max(1, nmain // max(1, args.oracle_samples))
+        errs, hows = [], set()
+        for k in range(0, nmain, k_s):
+            ref, how = oracle_solution(probs[k], threads)
+            errs.append(_rel(u_main[k], ref))
+            hows.add(how)
+        out["rel_err_max_sample"] = max(errs)
+        out["rel_err_reference"] = f"oracle on every {k_s}th request ({len(errs)}): " + "; ".join(sorted(hows))
+    # the same request set on FP64 and mixed servers (closed loop, all submitted at once)
+    comp = probs[: args.serve_compare]
+    cdofs = float(sum(p.n_dof for p in comp))
+    arms = {}
+    for precision, precond in (("fp64", "block_jacobi"), ("mixed", "block_jacobi"), ("mixed", "multigrid")):
+        s2 = server(precision, precond)
+        try:
+            _serve_closed(s2, comp)                # every topology's pattern built and cached
+            outs, w = _serve_closed(s2, comp)
+        finally:
+            s2.close()
+        its = np.array([r["iterations"] for _, r in outs])
+        arms[f"{precision}_{precond}"] = {"solves_per_s": len(comp) / w, "dof_per_s": cdofs / w, "wall_s": w,
+                                           "iterations_median": float(np.median(its)),
+                                           "statuses_ok": int(sum(r["status"] == 0 for _, r in outs))}
+    f64, mbj, mmg = arms["fp64_block_jacobi"], arms["mixed_block_jacobi"], arms["mixed_multigrid"]
+    out["compare"] = {"requests": len(comp), "arms": arms,
+                      "speedup_factors": {"precision": f64["wall_s"] / mbj["wall_s"],
+                                          "preconditioner": mbj["wall_s"] / mmg["wall_s"],
+                                          "both": f64["wall_s"] / mmg["wall_s"],
+                                          "basis": "wall time of the same requests submitted at once to a server "
+                                                   "of each kind, second pass (every topology cached)"}}
+    # bitwise repeats: a small pool served alone, then again in a shuffled mix
+    pool = [p for _, p in pkg.meshgen.serving_stream(24, seed=2007)]
+    s3 = server()
+    try:
+        first, _ = _serve_closed(s3, pool)
+        order = np.random.default_rng(3).permutation(len(pool))
+        again, _ = _serve_closed(s3, [pool[i] for i in order])
+    finally:
+        s3.close()
+    same = sum(bool(np.array_equal(again[j][0], first[i][0])) for j, i in enumerate(order))
+    out["repeat_bitwise_identical"] = f"{same}/{len(pool)}"
+    out["speedup_vs_fp64_server"] = f64["wall_s"] / mmg["wall_s"]
+    return out
+
+
+def _backlog(arrivals, recs):
+    """Largest number of requests submitted but not finished (host clock),
+    sampled at every arrival."""
+    ends = np.sort(np.array([arrivals[k] + r["total_ms"] * 1e-3 for k, _, r in recs]))
+    return int(max(i + 1 - np.searchsorted(ends, t, side="right") for i, t in enumerate(arrivals)))
 
 
 def main(argv=None):
