@@ -283,7 +283,12 @@ SFEM_API int sfem_batch_set_launch(sfem_batch *batch, int threads, int ctas_per_
  *   in its ID numbering.
  *   opts: precision, precond, rtol, maxit, reliable_delta are used.
  *   stats: nmesh entries (may be NULL).  The call returns SFEM_OK when the
- *   launch ran; per-mesh outcomes are in stats. */
+ *   launch ran; per-mesh outcomes are in stats.
+ * The device work of a call is one CUDA graph launch: uploads from device or
+ * pinned host memory, the persistent kernel, and the copy of u to device or
+ * pinned host memory (pageable host arrays are copied before and after it).
+ * The graph is captured at the first call and re-launched while the
+ * options, launch shape, argument lengths and those pointers stay the same. */
 SFEM_API int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *batch, int plane, const double *Young,
                               int64_t nYoung, const double *nu, int64_t nNu,
                               const int64_t *fix_offsets, const int64_t *fixed_dofs,

@@ -57,6 +57,14 @@ struct sfem_batch {
     std::vector<int> h_mg_ne;            // elements per direction of each structured mesh, else 0
     char *mg_buf = nullptr;              // every hierarchy's arrays
     MgMesh *mg_rec = nullptr;            // device: one record per mesh (nlev 0: no hierarchy)
+    // per-solve state: the host copy of the per-mesh table (its fixed-DOF
+    // ranges change per solve), pinned staging for it and for the statistics,
+    // and the CUDA graph of the last solve with the key it was captured for
+    std::vector<BatchMesh> h_meshes;
+    BatchMesh *h_tab = nullptr;
+    sfem_batch_stats *d_stats = nullptr, *h_stats = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> gkey;
 };
 
 namespace {
@@ -352,6 +360,14 @@ extern "C" int sfem_batch_create(sfem_ctx *ctx, int ndim, int function_class, in
         if ((st = sfem_dalloc(ctx, (void **)&bt->order, sizeof(int) * nmesh, "batch order"))) break;
         if ((st = sfem_dalloc(ctx, (void **)&bt->queue, 2 * sizeof(unsigned), "batch queue"))) break;
         if ((st = sfem_copy_in(ctx, bt->meshes, hm.data(), sizeof(BatchMesh) * nmesh, SFEM_MEM_HOST))) break;
+        bt->h_meshes = hm;
+        if ((st = sfem_cuda_status(ctx, cudaMallocHost((void **)&bt->h_tab, sizeof(BatchMesh) * nmesh),
+                                   "pinned batch table")))
+            break;
+        if ((st = sfem_cuda_status(ctx, cudaMallocHost((void **)&bt->h_stats, sizeof(sfem_batch_stats) * nmesh),
+                                   "pinned batch statistics")))
+            break;
+        if ((st = sfem_dalloc(ctx, (void **)&bt->d_stats, sizeof(sfem_batch_stats) * nmesh, "batch stats"))) break;
         if ((st = sfem_copy_in(ctx, bt->order, order.data(), sizeof(int) * nmesh, SFEM_MEM_HOST))) break;
         st = sfem_check_device(ctx, "batch create");
     } while (0);
@@ -487,11 +503,31 @@ static int grow(sfem_ctx *ctx, void **p, int64_t *cap, int64_t need, size_t elem
     return SFEM_OK;
 }
 
-// Copy material and boundary data into the batch's buffers and record each
-// mesh's fixed-DOF range.
+// A copy between a caller's pointer and the batch's buffers.  Copies from
+// or to device memory or pinned host memory run inside the solve's graph;
+// pageable host memory is copied outside it (a graph cannot copy from it).
+struct GCopy {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+
+static bool graph_copyable(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeHost;
+}
+
+// Check the material and boundary data, size the batch's buffers, and set
+// up the copies into them: pageable sources are copied now (ordered before
+// the solve on the stream), the others are returned in `in` for the graph.
+// The per-mesh table gets each mesh's fixed-DOF range from the host copy.
 static int batch_upload(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *Young, int64_t *nYoung,
                         const double *nu, int64_t *nNu, const int64_t *fix_offsets, const int64_t *fixed_dofs,
-                        const double *fixed_vals, int mem_space) {
+                        const double *fixed_vals, int mem_space, std::vector<GCopy> *in) {
     if (plane != SFEM_PLANE_STRESS && plane != SFEM_PLANE_STRAIN) return sfem_set_error(ctx, SFEM_BAD_ARG, "bad plane");
     const int64_t nm = bt->nmesh;
     if (bt->b > 1) {
@@ -504,7 +540,8 @@ static int batch_upload(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *
     }
     SFEM_TRY(sfem_check_ptr(ctx, fix_offsets, mem_space));
     std::vector<int64_t> fo(nm + 1);
-    SFEM_CUDA(ctx, cudaMemcpy(fo.data(), fix_offsets, sizeof(int64_t) * (nm + 1), cudaMemcpyDefault));
+    if (mem_space == SFEM_MEM_HOST) memcpy(fo.data(), fix_offsets, sizeof(int64_t) * (nm + 1));
+    else SFEM_CUDA(ctx, cudaMemcpy(fo.data(), fix_offsets, sizeof(int64_t) * (nm + 1), cudaMemcpyDeviceToHost));
     if (fo[0] != 0) return sfem_set_error(ctx, SFEM_BAD_ARG, "fix_offsets must start at 0");
     for (int64_t m = 0; m < nm; ++m)
         if (fo[m + 1] < fo[m]) return sfem_set_error(ctx, SFEM_BAD_ARG, "fix_offsets must not decrease");
@@ -514,20 +551,35 @@ static int batch_upload(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *
     SFEM_TRY(grow(ctx, (void **)&bt->nu, &bt->cap_nu, *nNu, sizeof(double), "batch nu"));
     SFEM_TRY(grow(ctx, (void **)&bt->fdofs, &bt->cap_fixd, nfix, sizeof(int64_t), "batch fixed dofs"));
     SFEM_TRY(grow(ctx, (void **)&bt->fvals, &bt->cap_fixv, nfix, sizeof(double), "batch fixed values"));
+    auto add = [&](void *dst, const void *src, size_t bytes) -> int {
+        if (bytes == 0) return SFEM_OK;
+        SFEM_TRY(sfem_check_ptr(ctx, src, mem_space));
+        if (graph_copyable(src)) {
+            in->push_back({dst, src, bytes});
+            return SFEM_OK;
+        }
+        return sfem_cuda_status(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, ctx->stream), "upload");
+    };
     if (bt->b > 1) {
-        SFEM_TRY(sfem_copy_in(ctx, bt->E, Young, sizeof(double) * *nYoung, mem_space));
-        SFEM_TRY(sfem_copy_in(ctx, bt->nu, nu, sizeof(double) * *nNu, mem_space));
+        SFEM_TRY(add(bt->E, Young, sizeof(double) * *nYoung));
+        SFEM_TRY(add(bt->nu, nu, sizeof(double) * *nNu));
     }
-    SFEM_TRY(sfem_copy_in(ctx, bt->fdofs, fixed_dofs, sizeof(int64_t) * nfix, mem_space));
-    SFEM_TRY(sfem_copy_in(ctx, bt->fvals, fixed_vals, sizeof(double) * nfix, mem_space));
-    std::vector<BatchMesh> hm(nm);
-    SFEM_CUDA(ctx, cudaMemcpyAsync(hm.data(), bt->meshes, sizeof(BatchMesh) * nm, cudaMemcpyDeviceToHost, ctx->stream));
-    SFEM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SFEM_TRY(add(bt->fdofs, fixed_dofs, sizeof(int64_t) * nfix));
+    SFEM_TRY(add(bt->fvals, fixed_vals, sizeof(double) * nfix));
+    // the previous solve has finished (solves end with a stream synchronise),
+    // so the pinned table can be rewritten
     for (int64_t m = 0; m < nm; ++m) {
-        hm[m].fix0 = fo[m];
-        hm[m].fix1 = fo[m + 1];
+        bt->h_meshes[m].fix0 = fo[m];
+        bt->h_meshes[m].fix1 = fo[m + 1];
     }
-    SFEM_CUDA(ctx, cudaMemcpyAsync(bt->meshes, hm.data(), sizeof(BatchMesh) * nm, cudaMemcpyHostToDevice, ctx->stream));
+    memcpy(bt->h_tab, bt->h_meshes.data(), sizeof(BatchMesh) * nm);
+    in->push_back({bt->meshes, bt->h_tab, sizeof(BatchMesh) * nm});
+    return SFEM_OK;
+}
+
+static int run_copies(sfem_ctx *ctx, const std::vector<GCopy> &cs) {
+    for (const GCopy &c : cs)
+        SFEM_CUDA(ctx, cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDefault, ctx->stream));
     return SFEM_OK;
 }
 
@@ -600,6 +652,18 @@ static int batch_opts(sfem_ctx *ctx, const sfem_solve_opts *opts, sfem_solve_opt
     return SFEM_OK;
 }
 
+template <typename V>
+static void key_put(std::vector<unsigned char> &k, const V &v) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(&v);
+    k.insert(k.end(), p, p + sizeof(V));
+}
+
+// One solve = one CUDA graph launch: the uploads from device or pinned
+// memory, the clearing of u and of the work queue, the persistent kernel, and
+// the copies of u (to device or pinned memory) and of the statistics.  The
+// graph is captured at the first solve and launched again as long as
+// nothing it holds changes (options, launch shape, buffer addresses, the
+// caller's device or pinned pointers); otherwise it is captured anew.
 extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const double *Young, int64_t nYoung,
                                 const double *nu, int64_t nNu, const int64_t *fix_offsets, const int64_t *fixed_dofs,
                                 const double *fixed_vals, double *u_out, int mem_space, const sfem_solve_opts *opts,
@@ -609,19 +673,73 @@ extern "C" int sfem_batch_solve(sfem_ctx *ctx, sfem_batch *bt, int plane, const 
     cudaSetDevice(ctx->device);
     sfem_solve_opts o;
     SFEM_TRY(batch_opts(ctx, opts, &o));
-    SFEM_TRY(batch_upload(ctx, bt, plane, Young, &nYoung, nu, &nNu, fix_offsets, fixed_dofs, fixed_vals, mem_space));
+    std::vector<GCopy> in;
+    SFEM_TRY(batch_upload(ctx, bt, plane, Young, &nYoung, nu, &nNu, fix_offsets, fixed_dofs, fixed_vals, mem_space,
+                          &in));
+    SFEM_TRY(sfem_check_ptr(ctx, u_out, mem_space));
+    if (o.precond == SFEM_PC_MULTIGRID && o.precision == SFEM_MIXED) SFEM_TRY(batch_mg(ctx, bt));  // allocates once
     const int64_t nm = bt->nmesh;
-    sfem_batch_stats *dstats = nullptr;
-    SFEM_TRY(sfem_dalloc(ctx, (void **)&dstats, sizeof(sfem_batch_stats) * nm, "batch stats"));
-    SFEM_CUDA(ctx, cudaMemsetAsync(bt->u, 0, sizeof(double) * (bt->total_dofs + 1), ctx->stream));
-    int st = batch_run(ctx, bt, o, plane, nYoung, nNu, bt->order, nm, bt->h_nodes.data(), dstats);
-    if (st == SFEM_OK) st = sfem_copy_out(ctx, u_out, bt->u, sizeof(double) * bt->total_dofs, mem_space);
-    if (st == SFEM_OK && stats)
-        st = sfem_cuda_status(ctx, cudaMemcpyAsync(stats, dstats, sizeof(sfem_batch_stats) * nm, cudaMemcpyDefault,
-                                                   ctx->stream),
-                              "stats copy");
+    const size_t ubytes = sizeof(double) * bt->total_dofs;
+    const bool u_in_graph = graph_copyable(u_out);
+    std::vector<unsigned char> key;
+    key_put(key, o.precision);
+    key_put(key, o.precond);
+    key_put(key, o.rtol);
+    key_put(key, o.maxit);
+    key_put(key, o.reliable_delta);
+    key_put(key, plane);
+    key_put(key, nYoung);
+    key_put(key, nNu);
+    key_put(key, bt->threads);
+    key_put(key, bt->ctas_per_sm);
+    key_put(key, bt->cluster);
+    key_put(key, bt->big_nodes);
+    key_put(key, (const void *)bt->E);
+    key_put(key, (const void *)bt->nu);
+    key_put(key, (const void *)bt->fdofs);
+    key_put(key, (const void *)bt->fvals);
+    key_put(key, (const void *)bt->mg_rec);
+    key_put(key, bt->mg_any);
+    for (const GCopy &c : in) key_put(key, c);
+    key_put(key, u_in_graph ? (const void *)u_out : nullptr);
+    if (!bt->gexec || key != bt->gkey) {
+        if (bt->gexec) cudaGraphExecDestroy(bt->gexec);
+        bt->gexec = nullptr;
+        bt->gkey.clear();
+        const long long launches = ctx->launches;
+        SFEM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int st = run_copies(ctx, in);
+        if (st == SFEM_OK)
+            st = sfem_cuda_status(ctx, cudaMemsetAsync(bt->u, 0, sizeof(double) * (bt->total_dofs + 1), ctx->stream),
+                                  "memset");
+        if (st == SFEM_OK) st = batch_run(ctx, bt, o, plane, nYoung, nNu, bt->order, nm, bt->h_nodes.data(), bt->d_stats);
+        if (st == SFEM_OK && u_in_graph)
+            st = sfem_cuda_status(ctx, cudaMemcpyAsync(u_out, bt->u, ubytes, cudaMemcpyDefault, ctx->stream), "copy-out");
+        if (st == SFEM_OK)
+            st = sfem_cuda_status(ctx, cudaMemcpyAsync(bt->h_stats, bt->d_stats, sizeof(sfem_batch_stats) * nm,
+                                                       cudaMemcpyDeviceToHost, ctx->stream),
+                                  "stats copy");
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+        ctx->launches = launches;  // counted per graph launch below
+        if (st == SFEM_OK && ec != cudaSuccess) st = sfem_cuda_status(ctx, ec, "batch graph capture");
+        if (st == SFEM_OK) st = sfem_cuda_status(ctx, cudaGraphInstantiate(&bt->gexec, g, 0), "batch graph instantiate");
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        if (st != SFEM_OK) {
+            bt->gexec = nullptr;
+            cudaStreamSynchronize(ctx->stream);
+            return st;
+        }
+        bt->gkey = key;
+    }
+    int st = sfem_cuda_status(ctx, cudaGraphLaunch(bt->gexec, ctx->stream), "batch graph launch");
+    if (st == SFEM_OK) ctx->launches += 1;
+    if (st == SFEM_OK && !u_in_graph) st = sfem_copy_out(ctx, u_out, bt->u, ubytes, mem_space);
     if (st == SFEM_OK) st = sfem_check_device(ctx, "batch solve");
-    sfem_dfree(ctx, dstats);
+    if (st == SFEM_OK && stats)
+        st = sfem_cuda_status(ctx, cudaMemcpy(stats, bt->h_stats, sizeof(sfem_batch_stats) * nm, cudaMemcpyDefault),
+                              "stats copy");
     cudaStreamSynchronize(ctx->stream);
     return st;
 }
@@ -637,7 +755,10 @@ extern "C" int sfem_batch_autotune(sfem_ctx *ctx, sfem_batch *bt, int plane, con
     cudaSetDevice(ctx->device);
     sfem_solve_opts o;
     SFEM_TRY(batch_opts(ctx, opts, &o));
-    SFEM_TRY(batch_upload(ctx, bt, plane, Young, &nYoung, nu, &nNu, fix_offsets, fixed_dofs, fixed_vals, mem_space));
+    std::vector<GCopy> in;
+    SFEM_TRY(batch_upload(ctx, bt, plane, Young, &nYoung, nu, &nNu, fix_offsets, fixed_dofs, fixed_vals, mem_space,
+                          &in));
+    SFEM_TRY(run_copies(ctx, in));
     const int64_t nm = bt->nmesh;
     const int64_t stride = std::max<int64_t>(1, sample > 0 ? nm / sample : 1);
     std::vector<int> horder(nm);
@@ -726,8 +847,12 @@ extern "C" int sfem_batch_destroy(sfem_batch *bt) {
                     bt->q64, bt->vecT, bt->fixed, bt->gfixed, bt->E, bt->nu, bt->fvals, bt->u, bt->fdofs,
                     bt->fix_off_dev, bt->mg_buf, bt->mg_rec};
     for (void *p : bufs) sfem_dfree(ctx, p);
+    sfem_dfree(ctx, bt->d_stats);
+    if (bt->gexec) cudaGraphExecDestroy(bt->gexec);
     if (bt->mesh) sfem_mesh_release(bt->mesh);
     cudaStreamSynchronize(ctx->stream);
+    if (bt->h_tab) cudaFreeHost(bt->h_tab);
+    if (bt->h_stats) cudaFreeHost(bt->h_stats);
     delete bt;
     return SFEM_OK;
 }
