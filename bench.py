@@ -109,7 +109,7 @@ def parse_args(argv=None):
                          "the FP32 residual 10x in 2-3 iterations; 0.01 halves the FP64 refreshes at the same error")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
     ap.add_argument("--serve-requests", type=int, default=960, help="requests in the configured-rate stream")
-    ap.add_argument("--serve-compare", type=int, default=96,
+    ap.add_argument("--serve-compare", type=int, default=64,
                     help="requests of the FP64 / mixed server comparison (submitted at once)")
     ap.add_argument("--serve-launch", default="8,256", help="cluster,threads of the serving kernel")
     ap.add_argument("--oracle-samples", type=int, default=16,
@@ -800,8 +800,8 @@ def batch_leg(args, pkg, ctx, stream, dist, threads):
             if args.batch_launch:
                 bt.set_launch(*[int(x) for x in args.batch_launch.split(",")])
                 shape = bt.launch()
-            else:  # full solves of an eighth of the meshes, taken evenly from the size order
-                shape, _ = bt.autotune(1.0, nus, fixed, vals, sample=max(1, len(probs) // 8), **kw)
+            else:  # full solves of a sixteenth of the meshes, taken evenly from the size order
+                shape, _ = bt.autotune(1.0, nus, fixed, vals, sample=max(1, len(probs) // 16), **kw)
             t_tune = time.perf_counter() - t0
             ms, outs = _timed_events(stream, lambda: bt.solve(1.0, nus, fixed, vals, **kw),
                                      args.leg_steps, min(args.leg_warmup, 1), dist)
@@ -1070,6 +1070,8 @@ def serve_leg(args, pkg, ctx, dist, threads):
         out["rel_err_reference"] = f"oracle on every {k_s}th request ({len(errs)}): " + "; ".join(sorted(hows))
     # the same request set on FP64 and mixed servers (closed loop, all submitted at once)
     comp = probs[: args.serve_compare]
+    if not comp:
+        return out
     cdofs = float(sum(p.n_dof for p in comp))
     arms = {}
     for precision, precond in (("fp64", "block_jacobi"), ("mixed", "block_jacobi"), ("mixed", "multigrid")):

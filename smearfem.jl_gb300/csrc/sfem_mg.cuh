@@ -44,9 +44,17 @@ struct MgLevel {
     float *x, *b, *t;   // iterate, right-hand side (levels >= 1), residual / smoothed iterate
 };
 
+// Levels at or below this size (with a next-finer level of at most
+// MG_SOLO_FINE nodes) are run by one CTA of a group when a thread-block
+// cluster works on the mesh: a CTA barrier costs a fraction of a cluster
+// barrier, and the few hundred nodes of such a level keep one CTA busy.
+constexpr int MG_SOLO_NODES = 1024;
+constexpr int MG_SOLO_FINE = 8192;
+
 struct MgMesh {
     int nlev;  // levels, the fine one included (>= 2)
     int ndc;   // DOFs of the coarsest level
+    int solo;  // first level run by one CTA of a cluster group (nlev: none)
     MgLevel lev[MG_MAX_LEVELS];
     float *cinv;  // inverse of the coarsest operator [ndc][ndc]; fixed rows and columns zero
     double *gj;   // Gauss-Jordan scratch [ndc][2 ndc]
@@ -97,6 +105,11 @@ inline int64_t mg_layout(int ndim, int B, int ne, int64_t ndp, char *base, MgMes
         }
         if (l == L - 1) m.ndc = (int)(nn * B);
         n = (n + 1) / 2;
+    }
+    m.solo = L;
+    for (int l = L - 1; l >= 1; --l) {
+        if (m.lev[l].nnode > MG_SOLO_NODES || m.lev[l - 1].nnode > MG_SOLO_FINE) break;
+        m.solo = l;
     }
     m.cinv = (float *)take(sizeof(float) * (int64_t)m.ndc * m.ndc);
     m.gj = (double *)take(sizeof(double) * 2 * (int64_t)m.ndc * m.ndc);
@@ -707,6 +720,11 @@ __device__ __forceinline__ void mg_stencil_pass(const MgLevel &C, float *out, in
 // z = V(r): one V(1,1) cycle on the residual r (FP32, the CG's).  On entry
 // the fine level's x holds the pre-smoothing sweep W D^-1 r (written by the
 // caller's vector update).  Returns this thread's r.z share.
+// In a cluster group, the levels from mgp->solo down (restriction into it,
+// the coarse solve, and back up to its smoothing) are run by the group's
+// first CTA alone with CTA barriers, while the others wait at one cluster
+// barrier; each pass computes the same values whoever runs it, so the
+// result does not change.
 template <class Grp, int NDIM, int B, int U, int W>
 __device__ __noinline__ double mg_vcycle(const Grp &G, const BatchArgs &a, const BatchMesh &M, const MgMesh *mgp,
                                          const float *r, float *z) {
@@ -715,12 +733,13 @@ __device__ __noinline__ double mg_vcycle(const Grp &G, const BatchArgs &a, const
     const int64_t gw = (int64_t)G.rank() * nw + (tid >> 5), gnw = (int64_t)G.size() * nw;
     const int64_t n1 = M.node0 + M.nnode;
     const int L = mgp->nlev;
+    const int S = G.size() > 1 ? min(max(mgp->solo, 1), L) : L;  // one CTA alone: nothing to hand over
     const MgLevel F0 = mgp->lev[0];
     // fine residual t0 = r - A x0
     grp_spmv<float, B, false, U, W, SPMV_RES>(a.sliceptr, a.col, a.val32, M.slice0 + gw, M.slice1, gnw, n1, F0.x,
                                               nullptr, 0.0f, nullptr, F0.t, a.fixed, true, r, nullptr);
     G.sync();
-    for (int l = 1; l < L; ++l) {
+    for (int l = 1; l < S; ++l) {
         const MgLevel F = mgp->lev[l - 1], C = mgp->lev[l];
         mg_restrict<NDIM, B>(M, F, C, l - 1, l + 1 < L, gt, gstride);
         G.sync();
@@ -729,10 +748,37 @@ __device__ __noinline__ double mg_vcycle(const Grp &G, const BatchArgs &a, const
             G.sync();
         }
     }
-    mg_coarse_solve(mgp->lev[L - 1], mgp->ndc, mgp->cinv, gt, gstride);  // coarsest: x = C^-1 b
-    G.sync();
     const float *xin = mgp->lev[L - 1].x;
-    for (int l = L - 2; l >= 1; --l) {
+    if (S < L) {
+        if (G.rank() == 0) {
+            const int64_t st = tid, ss = blockDim.x;
+            for (int l = S; l < L; ++l) {
+                const MgLevel F = mgp->lev[l - 1], C = mgp->lev[l];
+                mg_restrict<NDIM, B>(M, F, C, l - 1, l + 1 < L, st, ss);
+                __syncthreads();
+                if (l + 1 < L) {
+                    mg_stencil_pass<NDIM, B, SPMV_RES>(C, C.t, st, ss);
+                    __syncthreads();
+                }
+            }
+            mg_coarse_solve(mgp->lev[L - 1], mgp->ndc, mgp->cinv, st, ss);
+            __syncthreads();
+            for (int l = L - 2; l >= S; --l) {
+                const MgLevel F = mgp->lev[l], C = mgp->lev[l + 1];
+                mg_prolong<NDIM, B>(a, M, F, C, l, xin, st, ss);
+                __syncthreads();
+                mg_stencil_pass<NDIM, B, SPMV_SMOOTH>(F, F.t, st, ss);
+                __syncthreads();
+                xin = F.t;
+            }
+        }
+        G.sync();
+        xin = L - 2 >= S ? mgp->lev[S].t : mgp->lev[L - 1].x;
+    } else {
+        mg_coarse_solve(mgp->lev[L - 1], mgp->ndc, mgp->cinv, gt, gstride);  // coarsest: x = C^-1 b
+        G.sync();
+    }
+    for (int l = min(L - 2, S - 1); l >= 1; --l) {
         const MgLevel F = mgp->lev[l], C = mgp->lev[l + 1];
         mg_prolong<NDIM, B>(a, M, F, C, l, xin, gt, gstride);
         G.sync();
