@@ -804,8 +804,12 @@ def batch_leg(args, pkg, ctx, stream, dist, threads):
             if args.batch_launch:
                 bt.set_launch(*[int(x) for x in args.batch_launch.split(",")])
                 shape = bt.launch()
-            else:  # full solves of a sixteenth of the meshes, taken evenly from the size order
-                shape, _ = bt.autotune(1.0, nus, fixed, vals, sample=max(1, len(probs) // 16), **kw)
+            else:
+                # full solves of a sample taken evenly from the size order: every mesh for the
+                # multigrid arm (a batch solve takes ~0.4 s; a small sample favours larger
+                # clusters than the whole batch does), a sixteenth for the block-Jacobi arms
+                frac = 1 if precond == "multigrid" else 16
+                shape, _ = bt.autotune(1.0, nus, fixed, vals, sample=max(1, len(probs) // frac), **kw)
             t_tune = time.perf_counter() - t0
             ms, outs = _timed_events(stream, lambda: bt.solve(1.0, nus, fixed, vals, **kw),
                                      args.leg_steps, min(args.leg_warmup, 1), dist)

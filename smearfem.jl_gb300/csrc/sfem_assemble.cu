@@ -6,6 +6,8 @@
 //    and dN/dx = dN * inv(J) (:196) in FP64, into shared memory.  Then each
 //    thread accumulates, for a share of the element's node pairs (a <= b),
 //        S_ab = sum_gp w (dN_a/dx) (dN_b/dx)^T            (ndim x ndim)
+//    (for elasticity the shared gradients are stored scaled by sqrt(w), so
+//    each term is one product: 9 FMA per pair and Gauss point in 3D)
 //    and turns it into the elasticity block
 //        K_ab[i][j] = lambda S_ab[i][j] + mu S_ab[j][i] + mu delta_ij tr(S_ab),
 //    which is B_a' D B_b for the isotropic D of src/fem.jl:217 (plane stress)
@@ -90,6 +92,9 @@ k_element(const __grid_constant__ ElemTable tab, const double *__restrict__ X, c
         if (det == 0.0) sfem_dev_error(err, SFEM_SINGULAR_JACOBIAN, e);
         if (det < 0.0) atomicAdd(&err->neg_det, 1ull);
         double *g = sG + ((int64_t)gp * 32 + lane) * GS;
+        // elasticity stores sqrt(w |det J|) dN/dx, so that each Gauss point's
+        // term of a pair's block is a plain product (no weight per pair)
+        const double sc = B > 1 ? sqrt(tab.w[gp] * fabs(det)) : 1.0;
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
 #pragma unroll
@@ -97,7 +102,7 @@ k_element(const __grid_constant__ ElemTable tab, const double *__restrict__ X, c
                 double s = 0.0;
 #pragma unroll
                 for (int j = 0; j < NDIM; ++j) s = fma(tab.dN[gp][a][j], inv[j][k], s);
-                g[a * NDIM + k] = s;
+                g[a * NDIM + k] = B > 1 ? s * sc : s;
             }
         sW[gp * 32 + lane] = tab.w[gp] * fabs(det);
     }
@@ -138,10 +143,9 @@ k_element(const __grid_constant__ ElemTable tab, const double *__restrict__ X, c
 #pragma unroll
             for (int q = 0; q < NGP; ++q) {
                 const double *g = sG + ((int64_t)q * 32 + lane) * GS;
-                const double wq = sW[q * 32 + lane];
 #pragma unroll
                 for (int i = 0; i < NDIM; ++i) {
-                    const double wa = wq * g[a * NDIM + i];
+                    const double wa = g[a * NDIM + i];
 #pragma unroll
                     for (int j = 0; j < NDIM; ++j) S[i][j] = fma(wa, g[bq * NDIM + j], S[i][j]);
                 }

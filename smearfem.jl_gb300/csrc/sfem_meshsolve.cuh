@@ -610,6 +610,8 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                 }
                 if (det == 0.0) sfem_dev_error(a.err, SFEM_SINGULAR_JACOBIAN, e);
                 double *g = sG + ((int64_t)gp * 32 + lane) * GS;
+                // elasticity: sqrt(w |det J|) dN/dx (see k_element)
+                const double sc = B > 1 ? sqrt(tab.w[gp] * fabs(det)) : 1.0;
 #pragma unroll
                 for (int an = 0; an < NEN; ++an)
 #pragma unroll
@@ -617,7 +619,7 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
                         double s = 0.0;
 #pragma unroll
                         for (int j = 0; j < NDIM; ++j) s = fma(tab.dN[gp][an][j], inv[j][k], s);
-                        g[an * NDIM + k] = s;
+                        g[an * NDIM + k] = B > 1 ? s * sc : s;
                     }
                 sW[gp * 32 + lane] = tab.w[gp] * fabs(det);
             }
@@ -659,10 +661,9 @@ __device__ __forceinline__ void process_mesh(const Grp &G, const ElemTableB &tab
 #pragma unroll
                         for (int qg = 0; qg < NGP; ++qg) {
                             const double *g = sG + ((int64_t)qg * 32 + lane) * GS;
-                            const double wq = sW[qg * 32 + lane];
 #pragma unroll
                             for (int i = 0; i < NDIM; ++i) {
-                                const double wa = wq * g[pa * NDIM + i];
+                                const double wa = g[pa * NDIM + i];
 #pragma unroll
                                 for (int j = 0; j < NDIM; ++j) S[i][j] = fma(wa, g[pb * NDIM + j], S[i][j]);
                             }
