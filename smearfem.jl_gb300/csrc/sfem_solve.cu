@@ -340,57 +340,118 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
 // MIXED: the recursive FP32 residual never ends the solve; reaching the
 // tolerance, dropping by delta since the last refresh, or hitting maxit
 // requests an FP64 refresh instead (k_fold / k_spmv MODE 2 / k_refresh).
-// One thread per node: a thread loads its node's B entries of x, p, q, r and
-// its nodal inverse, and keeps them in registers -- no shared-memory staging,
-// no barrier, B + B*B loads in flight per thread.  A warp's loads still cover
-// contiguous segments (32 consecutive nodes).
+// Each thread owns NPT = 16 bytes / sizeof(T) consecutive nodes (4 in FP32,
+// 2 in FP64): their B * NPT entries of x, p, q, r are B 16-byte vectors, and
+// their inverse blocks MW 16-byte vectors, so every load and store is a
+// 16-byte access and the block product needs no data from other threads.
+// (One node per thread issued four times the load instructions, with a
+// 12-byte stride, and filled the load queues.)  Nodes after the last whole
+// group are handled one per thread.
 // MGPRE (multigrid): z and minv are the fine level's pre-smoothing sweep and
 // smoother; r.z and beta are left to the cycle's last product.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using V = float4;
+    static constexpr int E = 4;
+};
+template <>
+struct Vec16<double> {
+    using V = double2;
+    static constexpr int E = 2;
+};
+
 template <typename T, int B, int PC, bool MIXED, bool MGPRE = false>
 __global__ void __launch_bounds__(UPD_T)
 k_update_node(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
               const T *__restrict__ q, const T *__restrict__ minv, CgScalars *S, double *partial) {
     if (S->done) return;
+    using V = typename Vec16<T>::V;
+    constexpr int NPT = Vec16<T>::E;                           // nodes per thread
+    constexpr int MW = (PC == 0 || B == 1) ? B : B * B;        // inverse entries per node
     const T alpha = (T)S->alpha;
     double rz = 0.0, rr = 0.0;
-    for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < nN;
-         node += (int64_t)gridDim.x * blockDim.x) {
-        T xv[B], pv[B], qv[B], rv[B], mv[PC == 0 || B == 1 ? B : B * B];
+    const int64_t ngrp = nN / NPT;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t g = tid0; g < ngrp; g += stride) {
+        V xv[B], pv[B], qv[B], rv[B], mv[MW];
+        const V *xs = reinterpret_cast<const V *>(x + g * NPT * B);
+        const V *ps = reinterpret_cast<const V *>(p + g * NPT * B);
+        const V *qs = reinterpret_cast<const V *>(q + g * NPT * B);
+        const V *rs = reinterpret_cast<const V *>(r + g * NPT * B);
+        const V *ms = reinterpret_cast<const V *>(minv + g * NPT * MW);
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            xv[k] = xs[k];
+            pv[k] = ps[k];
+            qv[k] = qs[k];
+            rv[k] = rs[k];
+        }
+#pragma unroll
+        for (int k = 0; k < MW; ++k) mv[k] = ms[k];
+        T *xe = reinterpret_cast<T *>(xv);
+        const T *pe = reinterpret_cast<const T *>(pv);
+        const T *qe = reinterpret_cast<const T *>(qv);
+        T *re = reinterpret_cast<T *>(rv);
+        const T *me = reinterpret_cast<const T *>(mv);
+#pragma unroll
+        for (int i = 0; i < NPT * B; ++i) {
+            xe[i] = fma(alpha, pe[i], xe[i]);
+            re[i] = fma(-alpha, qe[i], re[i]);
+        }
+        V zv[B];
+        T *ze = reinterpret_cast<T *>(zv);
+#pragma unroll
+        for (int n = 0; n < NPT; ++n)
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                T zi;
+                if (MW == B) {
+                    zi = me[n * B + i] * re[n * B + i];
+                } else {
+                    zi = T(0);
+#pragma unroll
+                    for (int j = 0; j < B; ++j) zi = fma(me[(n * B + i) * B + j], re[n * B + j], zi);
+                }
+                ze[n * B + i] = zi;
+                rz += (double)(re[n * B + i] * zi);
+                rr += (double)(re[n * B + i] * re[n * B + i]);
+            }
+        V *xd = reinterpret_cast<V *>(x + g * NPT * B);
+        V *rd = reinterpret_cast<V *>(r + g * NPT * B);
+        V *zd = reinterpret_cast<V *>(z + g * NPT * B);
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            xd[k] = xv[k];
+            rd[k] = rv[k];
+            zd[k] = zv[k];
+        }
+    }
+    // the last nN % NPT nodes, one per thread
+    for (int64_t node = ngrp * NPT + tid0; node < nN; node += stride) {
+        T rl[B];
 #pragma unroll
         for (int i = 0; i < B; ++i) {
             const int64_t d = node * B + i;
-            xv[i] = x[d];
-            pv[i] = p[d];
-            qv[i] = q[d];
-            rv[i] = r[d];
-        }
-        if (PC == 0 || B == 1) {
-#pragma unroll
-            for (int i = 0; i < B; ++i) mv[i] = minv[node * B + i];
-        } else {
-#pragma unroll
-            for (int e = 0; e < B * B; ++e) mv[e] = minv[node * B * B + e];
-        }
-#pragma unroll
-        for (int i = 0; i < B; ++i) {
-            const int64_t d = node * B + i;
-            x[d] = fma(alpha, pv[i], xv[i]);
-            rv[i] = fma(-alpha, qv[i], rv[i]);
-            r[d] = rv[i];
+            x[d] = fma(alpha, p[d], x[d]);
+            rl[i] = fma(-alpha, q[d], r[d]);
+            r[d] = rl[i];
         }
 #pragma unroll
         for (int i = 0; i < B; ++i) {
             T zi;
-            if (PC == 0 || B == 1) {
-                zi = mv[i] * rv[i];
+            if (MW == B) {
+                zi = minv[node * B + i] * rl[i];
             } else {
                 zi = T(0);
 #pragma unroll
-                for (int j = 0; j < B; ++j) zi = fma(mv[i * B + j], rv[j], zi);
+                for (int j = 0; j < B; ++j) zi = fma(minv[(node * B + i) * B + j], rl[j], zi);
             }
             z[node * B + i] = zi;
-            rz += (double)(rv[i] * zi);
-            rr += (double)(rv[i] * rv[i]);
+            rz += (double)(rl[i] * zi);
+            rr += (double)(rl[i] * rl[i]);
         }
     }
     double trz, trr;
