@@ -38,7 +38,7 @@ constexpr int MG_MAX_LEVELS = 12;
 struct MgLevel {
     int n;              // elements per direction
     int nnode;          // (n + 1)^ndim
-    float *A;           // levels >= 1: stencil blocks [s][B*B][nnode]
+    float *A;           // levels >= 1: stencil blocks, see mg_a
     float *minv;        // l1-scaled block-Jacobi inverse [nnode][B][B]
     unsigned char *fr;  // levels >= 1: 1 for a free DOF [nnode * B]
     float *x, *b, *t;   // iterate, right-hand side (levels >= 1), residual / smoothed iterate
@@ -99,7 +99,7 @@ inline int64_t mg_layout(int ndim, int B, int ne, int64_t ndp, char *base, MgMes
         v.x = (float *)take(sizeof(float) * nd);
         v.t = (float *)take(sizeof(float) * nd);
         if (l > 0) {
-            v.A = (float *)take(sizeof(float) * S * B * B * nn);
+            v.A = (float *)take(sizeof(float) * S * B * B * ((nn + 31) / 32 * 32));
             v.fr = (unsigned char *)take(nn * B);
             v.b = (float *)take(sizeof(float) * nd);
         }
@@ -188,6 +188,17 @@ __device__ __forceinline__ int mg_stencil(const int ci[3], const int cj[3]) {
     return NDIM == 3 ? (cj[2] - ci[2] + 1) * 9 + s : s;
 }
 
+// Position of entry e (row-major in the B x B block) of stencil block s of
+// node I in a coarse level's A: nodes in tiles of 32, each tile's S * B * B
+// entries in order with its 32 nodes contiguous.  A warp on 32 consecutive
+// nodes reads one contiguous run of S * B * B * 128 bytes, every load at a
+// fixed offset from the tile's start.  Off-grid neighbours' blocks are zero.
+template <int NDIM, int B>
+__device__ __forceinline__ int64_t mg_a(int64_t I, int s, int e) {
+    constexpr int S = NDIM == 2 ? 9 : 27;
+    return ((I >> 5) * (S * B * B) + s * B * B + e) * 32 + (I & 31);
+}
+
 // Block (slab, lane) of the fine K in FP32: the lane-contiguous FP32 copy of
 // the batch and serving pipeline (one vector load), else the FP64 sliced-ELL
 // values rounded.
@@ -259,7 +270,7 @@ __device__ __forceinline__ bool mg_block(const BatchArgs &a, const BatchMesh &M,
     } else {
         const int s = mg_stencil<NDIM>(ci, cj);
 #pragma unroll
-        for (int e = 0; e < B * B; ++e) blk[e] = L.A[((int64_t)s * B * B + e) * L.nnode + li];
+        for (int e = 0; e < B * B; ++e) blk[e] = L.A[mg_a<NDIM, B>(li, s, e)];
     }
     return true;
 }
@@ -441,7 +452,7 @@ __device__ __forceinline__ void mg_pass_galerkin(const BatchArgs &a, const Batch
                     if (!C.fr[I * B + i] || !C.fr[mg_index<NDIM>(cJ, C.n) * B + j]) acc[i * B + j] = 0.0f;
         }
 #pragma unroll
-        for (int e = 0; e < B * B; ++e) C.A[((int64_t)s * B * B + e) * C.nnode + I] = acc[e];
+        for (int e = 0; e < B * B; ++e) C.A[mg_a<NDIM, B>(I, s, e)] = acc[e];
     }
 }
 
@@ -455,7 +466,7 @@ __device__ __forceinline__ void mg_pass_smoother(const MgLevel &C, int64_t gt, i
 #pragma unroll
         for (int c = 0; c < B; ++c) f[c] = C.fr[I * B + c] != 0;
 #pragma unroll
-        for (int e = 0; e < B * B; ++e) D[e] = C.A[((int64_t)(S / 2) * B * B + e) * C.nnode + I];
+        for (int e = 0; e < B * B; ++e) D[e] = C.A[mg_a<NDIM, B>(I, S / 2, e)];
         if (!mg_inv_block<B>(D, f, Di)) {
             atomicMax(flag, (int)SFEM_SINGULAR);
 #pragma unroll
@@ -467,7 +478,7 @@ __device__ __forceinline__ void mg_pass_smoother(const MgLevel &C, int64_t gt, i
         for (int s = 0; s < S; ++s) {
             float blk[B * B];
 #pragma unroll
-            for (int e = 0; e < B * B; ++e) blk[e] = C.A[((int64_t)s * B * B + e) * C.nnode + I];
+            for (int e = 0; e < B * B; ++e) blk[e] = C.A[mg_a<NDIM, B>(I, s, e)];
 #pragma unroll
             for (int i = 0; i < B; ++i)
 #pragma unroll
@@ -508,7 +519,7 @@ __device__ __forceinline__ void mg_pass_coarsest(const MgLevel &C, int n, float 
                 bool nb = true;
 #pragma unroll
                 for (int d = 0; d < NDIM; ++d) nb = nb && abs(cI[d] - cJ[d]) <= 1;
-                if (nb) v = C.A[((int64_t)mg_stencil<NDIM>(cI, cJ) * B * B + i * B + j) * C.nnode + I];
+                if (nb) v = C.A[mg_a<NDIM, B>(I, mg_stencil<NDIM>(cI, cJ), i * B + j)];
             }
         }
         g[q] = v;
@@ -542,6 +553,7 @@ __device__ __forceinline__ void mg_coarse_solve(const MgLevel &C, int n, const f
                                                 int64_t gstride) {
     for (int64_t q = gt; q < n; q += gstride) {
         float v = 0.0f;
+#pragma unroll 27
         for (int c = 0; c < n; ++c) v = fmaf(cinv[q * n + c], C.b[c], v);
         C.x[q] = v;
     }
@@ -569,39 +581,44 @@ __device__ __noinline__ void mg_setup(const Grp &G, const BatchArgs &a, const Ba
 
 // Restriction of level l's residual t_l into b_{l+1}; with `smooth`, also
 // the pre-smoothing sweep from zero x_{l+1} = W D^-1 b_{l+1}.
+// Every coarse node takes the same 3 (x 3 x 3) fine candidates, ascending,
+// the ones off the grid or outside its support with weight zero at a clamped
+// index: fixed trip counts let all loads of a node be in flight at once, and
+// the zero terms leave the sum unchanged.
 template <int NDIM, int B>
 __device__ __forceinline__ void mg_restrict(const BatchMesh &M, const MgLevel &F, const MgLevel &C, int l, bool smooth,
                                             int64_t gt, int64_t gstride) {
+    constexpr int KZ = NDIM == 3 ? 3 : 1;
     for (int64_t I = gt; I < C.nnode; I += gstride) {
         int cI[3];
         mg_coords<NDIM>(I, C.n, cI);
-        int fi[3][3], nf[3] = {1, 1, 1};
+        int fi[3][3];
         float fw[3][3];
-        fi[2][0] = 0;
-        fw[2][0] = 1.0f;
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
-            int k = 0;
-            const int cc = min(2 * cI[d], F.n);
-            for (int i = cc - 1; i <= cc + 1; ++i) {
-                if (i < 0 || i > F.n) continue;
-                const float w = mg_w1(i, cI[d], F.n);
-                if (w == 0.0f) continue;
-                fi[d][k] = i;
-                fw[d][k] = w;
-                ++k;
+        for (int d = 0; d < 3; ++d) {
+            const int cc = d < NDIM ? min(2 * cI[d], F.n) : 0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int i = cc - 1 + k;
+                const bool in = d < NDIM ? (i >= 0 && i <= F.n) : k == 1;
+                fi[d][k] = min(max(i, 0), d < NDIM ? F.n : 0);
+                fw[d][k] = !in ? 0.0f : (d < NDIM ? mg_w1(i, cI[d], F.n) : 1.0f);
             }
-            nf[d] = k;
         }
         float acc[B];
 #pragma unroll
         for (int c = 0; c < B; ++c) acc[c] = 0.0f;
-        for (int kz = 0; kz < nf[2]; ++kz)
-            for (int ky = 0; ky < nf[1]; ++ky)
-                for (int kx = 0; kx < nf[0]; ++kx) {
-                    const int ci[3] = {fi[0][kx], fi[1][ky], fi[2][kz]};
-                    const float w = fw[0][kx] * fw[1][ky] * fw[2][kz];
-                    const int64_t li = mg_index<NDIM>(ci, F.n) + (l == 0 ? M.node0 : 0);
+        const int64_t off = l == 0 ? M.node0 : 0;
+#pragma unroll
+        for (int kz = 0; kz < KZ; ++kz)
+#pragma unroll
+            for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+                for (int kx = 0; kx < 3; ++kx) {
+                    const int zk = NDIM == 3 ? kz : 1;
+                    const int ci[3] = {fi[0][kx], fi[1][ky], fi[2][zk]};
+                    const float w = fw[0][kx] * fw[1][ky] * fw[2][zk];
+                    const int64_t li = mg_index<NDIM>(ci, F.n) + off;
 #pragma unroll
                     for (int c = 0; c < B; ++c) acc[c] = fmaf(w, F.t[li * B + c], acc[c]);  // t = 0 on fixed DOFs
                 }
@@ -622,41 +639,44 @@ __device__ __forceinline__ void mg_restrict(const BatchMesh &M, const MgLevel &F
     }
 }
 
-// x_l += P' xc (xc: level l+1's iterate, zero on its fixed DOFs).
+// x_l += P' xc (xc: level l+1's iterate, zero on its fixed DOFs).  Two coarse
+// candidates per direction (the second with weight zero where the fine node
+// sits on a coarse one), for the same reason as in mg_restrict.
 template <int NDIM, int B>
 __device__ __forceinline__ void mg_prolong(const BatchArgs &a, const BatchMesh &M, const MgLevel &F, const MgLevel &C,
                                            int l, const float *xc, int64_t gt, int64_t gstride) {
+    constexpr int KZ = NDIM == 3 ? 2 : 1;
     for (int64_t li = gt; li < F.nnode; li += gstride) {
         int ci[3];
         mg_coords<NDIM>(li, F.n, ci);
-        int cc[3][2], nc[3] = {1, 1, 1};
+        int cc[3][2];
         float cw[3][2];
-        cc[2][0] = 0;
-        cw[2][0] = 1.0f;
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
+        for (int d = 0; d < 3; ++d) {
             const int i = ci[d];
-            if (i == F.n) {
-                cc[d][0] = C.n;
+            if (d >= NDIM) {
+                cc[d][0] = cc[d][1] = 0;
                 cw[d][0] = 1.0f;
-                nc[d] = 1;
-            } else if (!(i & 1)) {
-                cc[d][0] = i / 2;
+                cw[d][1] = 0.0f;
+            } else if (i == F.n || !(i & 1)) {
+                cc[d][0] = cc[d][1] = i == F.n ? C.n : i / 2;
                 cw[d][0] = 1.0f;
-                nc[d] = 1;
+                cw[d][1] = 0.0f;
             } else {
                 cc[d][0] = (i - 1) / 2;
                 cc[d][1] = (i + 1) / 2;
                 cw[d][0] = cw[d][1] = 0.5f;
-                nc[d] = 2;
             }
         }
         float acc[B];
 #pragma unroll
         for (int c = 0; c < B; ++c) acc[c] = 0.0f;
-        for (int kz = 0; kz < nc[2]; ++kz)
-            for (int ky = 0; ky < nc[1]; ++ky)
-                for (int kx = 0; kx < nc[0]; ++kx) {
+#pragma unroll
+        for (int kz = 0; kz < KZ; ++kz)
+#pragma unroll
+            for (int ky = 0; ky < 2; ++ky)
+#pragma unroll
+                for (int kx = 0; kx < 2; ++kx) {
                     const int cI[3] = {cc[0][kx], cc[1][ky], cc[2][kz]};
                     const float w = cw[0][kx] * cw[1][ky] * cw[2][kz];
                     const int64_t I = mg_index<NDIM>(cI, C.n);
@@ -683,13 +703,21 @@ __device__ __forceinline__ void mg_stencil_pass(const MgLevel &C, float *out, in
         float acc[B];
 #pragma unroll
         for (int c = 0; c < B; ++c) acc[c] = 0.0f;
-#pragma unroll 3
-        for (int s = 0; s < S; ++s) {
-            const int cJ[3] = {cI[0] + s % 3 - 1, cI[1] + (s / 3) % 3 - 1, NDIM == 3 ? cI[2] + s / 9 - 1 : 0};
-            bool valid = true;
+        const float *At = C.A + mg_a<NDIM, B>(I, 0, 0);
+        // off-grid neighbours are clamped onto the grid: their blocks are
+        // zero, so they add nothing and the sweep has no branch
+        int lo[3], hi[3];
 #pragma unroll
-            for (int d = 0; d < NDIM; ++d) valid = valid && cJ[d] >= 0 && cJ[d] <= C.n;
-            if (!valid) continue;
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = d < NDIM && cI[d] > 0 ? -1 : 0;
+            hi[d] = d < NDIM && cI[d] < C.n ? 1 : 0;
+        }
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, NDIM == 3 ? s / 9 - 1 : 0};
+            int cJ[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) cJ[d] = cI[d] + min(max(o[d], lo[d]), hi[d]);
             const int64_t J = mg_index<NDIM>(cJ, C.n);
             float xj[B];
 #pragma unroll
@@ -697,7 +725,7 @@ __device__ __forceinline__ void mg_stencil_pass(const MgLevel &C, float *out, in
 #pragma unroll
             for (int i = 0; i < B; ++i)
 #pragma unroll
-                for (int j = 0; j < B; ++j) acc[i] = fmaf(C.A[((int64_t)s * B * B + i * B + j) * C.nnode + I], xj[j], acc[i]);
+                for (int j = 0; j < B; ++j) acc[i] = fmaf(At[(s * B * B + i * B + j) * 32], xj[j], acc[i]);
         }
         float res[B];
 #pragma unroll

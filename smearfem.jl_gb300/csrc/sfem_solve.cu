@@ -821,6 +821,40 @@ __global__ void k_mg_csolve(const MgLevel C, int n, const float *cinv, const CgS
 }
 #undef SFEM_GRID_LOOP
 
+// The levels from `solo` down, their coarse solve and the way back up to
+// level solo's smoothing, by ONE CTA with CTA barriers: the few thousand
+// nodes of these levels keep one CTA busy, and one launch replaces two per
+// level (each of them bound by a few memory round trips, not by bytes).
+// The passes and their order are those of the grid-wide kernels.
+constexpr int MG_SOLO_T = 1024;
+constexpr int64_t MG_SOLO_MAX_NODES = 8192;  // largest level (and its finer neighbour / 8) run by the one CTA
+template <int NDIM, int B>
+__global__ void __launch_bounds__(MG_SOLO_T)
+k_mg_solo(const sfem_dev::BatchArgs a, const BatchMesh M, const __grid_constant__ MgMesh mg, int solo,
+          const CgScalars *S) {
+    if (S->done) return;
+    const int64_t st = threadIdx.x, ss = blockDim.x;
+    const int L = mg.nlev;
+    for (int l = solo; l < L; ++l) {
+        sfem_dev::mg_restrict<NDIM, B>(M, mg.lev[l - 1], mg.lev[l], l - 1, l + 1 < L, st, ss);
+        __syncthreads();
+        if (l + 1 < L) {
+            sfem_dev::mg_stencil_pass<NDIM, B, sfem_dev::SPMV_RES>(mg.lev[l], mg.lev[l].t, st, ss);
+            __syncthreads();
+        }
+    }
+    sfem_dev::mg_coarse_solve(mg.lev[L - 1], mg.ndc, mg.cinv, st, ss);
+    __syncthreads();
+    const float *xin = mg.lev[L - 1].x;
+    for (int l = L - 2; l >= solo; --l) {
+        sfem_dev::mg_prolong<NDIM, B>(a, M, mg.lev[l], mg.lev[l + 1], l, xin, st, ss);
+        __syncthreads();
+        sfem_dev::mg_stencil_pass<NDIM, B, sfem_dev::SPMV_SMOOTH>(mg.lev[l], mg.lev[l].t, st, ss);
+        __syncthreads();
+        xin = mg.lev[l].t;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
@@ -996,7 +1030,14 @@ int Solver::mg_cycle(const float *r, float *z) {
             nullptr, r, nullptr);
     }
     ++n;
-    for (int l = 1; l < L; ++l) {
+    // levels solo.. run by one CTA (k_mg_solo); solo = L: none
+    int solo = L;
+    for (int l = 2; l < L; ++l)
+        if (mg.lev[l].nnode <= MG_SOLO_MAX_NODES && mg.lev[l - 1].nnode <= 8 * MG_SOLO_MAX_NODES) {
+            solo = l;
+            break;
+        }
+    for (int l = 1; l < solo; ++l) {
         k_mg_restrict<NDIM, B><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mgM, mg.lev[l - 1], mg.lev[l], l - 1,
                                                                                l + 1 < L ? 1 : 0, S);
         ++n;
@@ -1005,10 +1046,16 @@ int Solver::mg_cycle(const float *r, float *z) {
             ++n;
         }
     }
-    k_mg_csolve<<<1, 256, 0, ctx->stream>>>(mg.lev[L - 1], mg.ndc, mg.cinv, S);
-    ++n;
     const float *xin = mg.lev[L - 1].x;
-    for (int l = L - 2; l >= 1; --l) {
+    if (solo < L) {
+        k_mg_solo<NDIM, B><<<1, MG_SOLO_T, 0, ctx->stream>>>(mga, mgM, mg, solo, S);
+        ++n;
+        if (solo <= L - 2) xin = mg.lev[solo].t;
+    } else {
+        k_mg_csolve<<<1, 256, 0, ctx->stream>>>(mg.lev[L - 1], mg.ndc, mg.cinv, S);
+        ++n;
+    }
+    for (int l = std::min(L - 2, solo - 1); l >= 1; --l) {
         k_mg_prolong<NDIM, B><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mga, mgM, mg.lev[l], mg.lev[l + 1], l,
                                                                               xin, S);
         k_mg_stencil<NDIM, B, SPMV_SMOOTH><<<grid(mg.lev[l].nnode), 256, 0, ctx->stream>>>(mg.lev[l], mg.lev[l].t, S);

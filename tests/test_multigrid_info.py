@@ -41,7 +41,7 @@ def _bytes(ndim, b, ne):
         take(4 * nd)
         take(4 * nd)
         if lvl > 0:
-            take(4 * S * b * b * nn)
+            take(4 * S * b * b * ((nn + 31) // 32 * 32))  # stencil blocks in tiles of 32 nodes
             take(nn * b)
             take(4 * nd)
         if lvl == L - 1:
