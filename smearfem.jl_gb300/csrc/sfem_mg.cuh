@@ -378,7 +378,35 @@ __device__ __forceinline__ void mg_pass_free(const BatchArgs &a, const BatchMesh
     }
 }
 
+// The pairs kx of one (kz, ky) row of the Galerkin sum on a stencil level,
+// NX of them (a fixed count, so that their loads are in flight together).
+template <int NDIM, int B, int NX>
+__device__ __forceinline__ void mg_galerkin_row(const MgLevel &F, const int (&pi)[3][7], const int (&pj)[3][7],
+                                                const float (&pw)[3][7], int ky, int kz, float *acc) {
+#pragma unroll
+    for (int kx = 0; kx < NX; ++kx) {
+        const int ci[3] = {pi[0][kx], pi[1][ky], pi[2][kz]};
+        const int cj[3] = {pj[0][kx], pj[1][ky], pj[2][kz]};
+        const float w = pw[0][kx] * pw[1][ky] * pw[2][kz];
+        const int64_t li = mg_index<NDIM>(ci, F.n), lj = mg_index<NDIM>(cj, F.n);
+        const int st = mg_stencil<NDIM>(ci, cj);
+        float blk[B * B];
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) blk[e] = F.A[mg_a<NDIM, B>(li, st, e)];
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j)
+                if (F.fr[li * B + i] && F.fr[lj * B + j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
+    }
+}
+
 // Galerkin product: one (coarse node, stencil neighbour) block per step.
+// On a stencil level (l >= 1) each direction's pair list is padded, after
+// its real pairs, with zero-weight pairs (i, i) to 7 (offset 0) or 3
+// (offset +-1) entries: the counts are the same for a warp's nodes, the
+// innermost loop has a fixed trip count, and the zero terms leave every sum
+// bitwise unchanged.
 template <int NDIM, int B>
 __device__ __forceinline__ void mg_pass_galerkin(const BatchArgs &a, const BatchMesh &M, const MgLevel &F,
                                                  const MgLevel &C, int l, int64_t gt, int64_t gstride, int *flag) {
@@ -423,28 +451,43 @@ __device__ __forceinline__ void mg_pass_galerkin(const BatchArgs &a, const Batch
                         ++k;
                     }
                 }
+                if (l >= 1) {
+                    const int npad = off[d] == 0 ? 7 : 3;
+                    for (; k < npad; ++k) {
+                        pi[d][k] = pj[d][k] = ccI;
+                        pw[d][k] = 0.0f;
+                    }
+                }
                 np[d] = k;
             }
-            for (int kz = 0; kz < np[2]; ++kz)
-                for (int ky = 0; ky < np[1]; ++ky)
-                    for (int kx = 0; kx < np[0]; ++kx) {
-                        const int ci[3] = {pi[0][kx], pi[1][ky], pi[2][kz]};
-                        const int cj[3] = {pj[0][kx], pj[1][ky], pj[2][kz]};
-                        const float w = pw[0][kx] * pw[1][ky] * pw[2][kz];
-                        float blk[B * B];
-                        if (!mg_block<NDIM, B>(a, M, F, l, ci, cj, blk)) {
-                            atomicMax(flag, (int)SFEM_BAD_INDEX);
-                            continue;
-                        }
-                        bool fi[B], fj[B];
-                        mg_free<NDIM, B>(a, M, F, l, ci, fi);
-                        mg_free<NDIM, B>(a, M, F, l, cj, fj);
-#pragma unroll
-                        for (int i = 0; i < B; ++i)
-#pragma unroll
-                            for (int j = 0; j < B; ++j)
-                                if (fi[i] && fj[j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
+            if (l >= 1) {
+                for (int kz = 0; kz < np[2]; ++kz)
+                    for (int ky = 0; ky < np[1]; ++ky) {
+                        if (np[0] == 7) mg_galerkin_row<NDIM, B, 7>(F, pi, pj, pw, ky, kz, acc);
+                        else mg_galerkin_row<NDIM, B, 3>(F, pi, pj, pw, ky, kz, acc);
                     }
+            } else {
+                for (int kz = 0; kz < np[2]; ++kz)
+                    for (int ky = 0; ky < np[1]; ++ky)
+                        for (int kx = 0; kx < np[0]; ++kx) {
+                            const int ci[3] = {pi[0][kx], pi[1][ky], pi[2][kz]};
+                            const int cj[3] = {pj[0][kx], pj[1][ky], pj[2][kz]};
+                            const float w = pw[0][kx] * pw[1][ky] * pw[2][kz];
+                            float blk[B * B];
+                            if (!mg_block<NDIM, B>(a, M, F, l, ci, cj, blk)) {
+                                atomicMax(flag, (int)SFEM_BAD_INDEX);
+                                continue;
+                            }
+                            bool fi[B], fj[B];
+                            mg_free<NDIM, B>(a, M, F, l, ci, fi);
+                            mg_free<NDIM, B>(a, M, F, l, cj, fj);
+#pragma unroll
+                            for (int i = 0; i < B; ++i)
+#pragma unroll
+                                for (int j = 0; j < B; ++j)
+                                    if (fi[i] && fj[j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
+                        }
+            }
 #pragma unroll
             for (int i = 0; i < B; ++i)
 #pragma unroll

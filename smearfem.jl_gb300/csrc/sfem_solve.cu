@@ -784,6 +784,69 @@ __global__ void k_mg_galerkin(const sfem_dev::BatchArgs a, const BatchMesh M, co
     SFEM_GRID_LOOP
     sfem_dev::mg_pass_galerkin<NDIM, B>(a, M, F, C, l, gt, gs, flag);
 }
+// Fine level as a stencil level for the Galerkin pass: F.A (tiled stencil
+// blocks, the FP32 values of the upper-triangle copy, lower blocks
+// transposed) and F.fr (free flags) from K's upper-triangle storage; one lane
+// per row, one warp per slice.  Off-grid neighbours get zero blocks; a
+// column that is not a grid neighbour sets SFEM_BAD_INDEX.
+template <int NDIM, int B>
+__global__ void k_mg_fine_stencil(const int64_t *__restrict__ sptrU, const int *__restrict__ colU,
+                                  const float *__restrict__ valU, const int64_t *__restrict__ sptrL,
+                                  const int2 *__restrict__ lo, const unsigned char *__restrict__ fixed, int64_t nslices,
+                                  const MgLevel F, int *flag) {
+    constexpr int S = NDIM == 2 ? 9 : 27;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t sl = t >> 5;
+    const int lane = (int)(t & 31);
+    if (sl >= nslices) return;
+    const int64_t r = sl * 32 + lane;
+    if (r >= F.nnode) return;
+    int ci[3];
+    sfem_dev::mg_coords<NDIM>(r, F.n, ci);
+    unsigned written = 0;
+    auto put = [&](int c, const float *blk, bool transpose) {
+        int cj[3];
+        sfem_dev::mg_coords<NDIM>(c, F.n, cj);
+        bool nb = true;
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) nb = nb && abs(cj[d] - ci[d]) <= 1;
+        if (!nb) {
+            atomicMax(flag, (int)SFEM_BAD_INDEX);
+            return;
+        }
+        const int st = sfem_dev::mg_stencil<NDIM>(ci, cj);
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j)
+                F.A[sfem_dev::mg_a<NDIM, B>(r, st, i * B + j)] = transpose ? blk[j * B + i] : blk[i * B + j];
+        written |= 1u << st;
+    };
+    const int64_t u0 = sptrU[sl], nu = sptrU[sl + 1] - u0;
+    for (int64_t k = 0; k < nu; ++k) {
+        const int c = colU[(u0 + k) * 32 + lane];
+        if (k > 0 && c == (int)r) continue;  // padding (the diagonal is the first upper entry)
+        float blk[B * B];
+        load_v32<B, false>(valU, u0 + k, lane, blk);
+        put(c, blk, false);
+    }
+    const int64_t l0 = sptrL[sl], nl = sptrL[sl + 1] - l0;
+    for (int64_t k = 0; k < nl; ++k) {
+        const int2 e = lo[(l0 + k) * 32 + lane];
+        if (e.x < 0) continue;
+        float blk[B * B];
+        load_v32<B, false>(valU, e.x >> 5, e.x & 31, blk);
+        put(e.y, blk, true);
+    }
+#pragma unroll
+    for (int st = 0; st < S; ++st)
+        if (!(written >> st & 1u))
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) F.A[sfem_dev::mg_a<NDIM, B>(r, st, e)] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < B; ++c) F.fr[r * B + c] = fixed[r * B + c] ? 0 : 1;
+}
+
 template <int NDIM, int B>
 __global__ void k_mg_smoother(const MgLevel C, int *flag) {
     SFEM_GRID_LOOP
@@ -994,10 +1057,32 @@ int Solver::mg_build(const float *bj) {
     auto grid = [&](int64_t work) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(sfem_cdiv(work, 256), 64 * ctx->num_sms)); };
     const int L = mg.nlev, S = NDIM == 2 ? 9 : 27;
     k_mg_fine<NDIM, B><<<grid(mg.lev[0].nnode), 256, 0, ctx->stream>>>(mga, mgM, mg.lev[0], bj);
+    // the fine level as a stencil level (scratch for this set-up): the
+    // Galerkin pass then reads each fine block with one load group
+    MgLevel F0 = mg.lev[0];
+    struct Scratch {  // freed in stream order when the set-up has been enqueued
+        sfem_ctx *ctx;
+        void *p[2] = {nullptr, nullptr};
+        ~Scratch() {
+            for (void *q : p) sfem_dfree(ctx, q);
+        }
+    } scratch{ctx};
+    {
+        const int64_t nn = (int64_t)F0.nnode;
+        SFEM_TRY(sfem_dalloc(ctx, &scratch.p[0], sizeof(float) * S * B * B * ((nn + 31) / 32 * 32),
+                             "multigrid fine stencil"));
+        SFEM_TRY(sfem_dalloc(ctx, &scratch.p[1], (size_t)(nn * B), "multigrid fine flags"));
+        F0.A = (float *)scratch.p[0];
+        F0.fr = (unsigned char *)scratch.p[1];
+        k_mg_fine_stencil<NDIM, B><<<(unsigned)sfem_cdiv(m->nslices * 32, 256), 256, 0, ctx->stream>>>(
+            K->sptrU, K->colU, K->valU, K->sptrL, K->lo, fixed, m->nslices, F0, flag);
+        ctx->launches += 2;
+    }
     for (int l = 0; l + 1 < L; ++l) {
         k_mg_free<NDIM, B><<<grid(mg.lev[l + 1].nnode), 256, 0, ctx->stream>>>(mga, mgM, mg.lev[l], mg.lev[l + 1], l);
+        // level 0 through its stencil copy (l = 1 selects the stencil path; the mesh starts at node 0)
         k_mg_galerkin<NDIM, B><<<grid((int64_t)mg.lev[l + 1].nnode * S), 256, 0, ctx->stream>>>(
-            mga, mgM, mg.lev[l], mg.lev[l + 1], l, flag);
+            mga, mgM, l == 0 ? F0 : mg.lev[l], mg.lev[l + 1], l == 0 ? 1 : l, flag);
         ctx->launches += 2;
         if (l + 2 < L) {
             k_mg_smoother<NDIM, B><<<grid(mg.lev[l + 1].nnode), 256, 0, ctx->stream>>>(mg.lev[l + 1], flag);
