@@ -142,12 +142,51 @@ __device__ int row_neighbours(int r, const int64_t *__restrict__ n2e_ptr, const 
     return k;
 }
 
+// The same selection with the node lists of up to MAXE incident elements
+// held in registers (loaded once, all loads in flight together); rows with
+// more incident elements take row_neighbours.
+template <int NEN, int MAXE>
+__device__ int row_neighbours_reg(int r, const int64_t *__restrict__ n2e_ptr, const int *__restrict__ n2e,
+                                  const int *__restrict__ ien, int64_t nEl, int *out, int64_t stride) {
+    const int64_t s = n2e_ptr[r], t = n2e_ptr[r + 1];
+    if (t - s > MAXE) return row_neighbours(r, n2e_ptr, n2e, ien, nEl, NEN, out, stride);
+    const int n = (int)(t - s);
+    int nodes[MAXE * NEN];
+#pragma unroll
+    for (int m = 0; m < MAXE; ++m) {
+        const int e = m < n ? n2e[s + m] : 0;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) nodes[m * NEN + a] = m < n ? __ldg(&ien[(int64_t)a * nEl + e]) : INT_MAX;
+    }
+    int prev = -1, k = 0;
+    while (true) {
+        int best = INT_MAX;
+#pragma unroll
+        for (int i = 0; i < MAXE * NEN; ++i) best = (nodes[i] > prev && nodes[i] < best) ? nodes[i] : best;
+        if (best == INT_MAX) break;
+        if (out) out[(int64_t)k * stride] = best;
+        prev = best;
+        ++k;
+    }
+    return k;
+}
+
+// NEN > 0: the register form for NEN nodes per element; NEN = 0: any nen.
+template <int NEN, int MAXE>
+__device__ __forceinline__ int row_neighbours_any(int r, const int64_t *__restrict__ n2e_ptr,
+                                                  const int *__restrict__ n2e, const int *__restrict__ ien,
+                                                  int64_t nEl, int nen, int *out, int64_t stride) {
+    if constexpr (NEN > 0) return row_neighbours_reg<NEN, MAXE>(r, n2e_ptr, n2e, ien, nEl, out, stride);
+    else return row_neighbours(r, n2e_ptr, n2e, ien, nEl, nen, out, stride);
+}
+
+template <int NEN, int MAXE>
 __global__ void k_rowlen(const int64_t *__restrict__ n2e_ptr, const int *__restrict__ n2e,
                          const int *__restrict__ ien, int64_t nEl, int nen, int64_t nN,
                          int *__restrict__ rowlen) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nN) return;
-    rowlen[r] = row_neighbours((int)r, n2e_ptr, n2e, ien, nEl, nen, nullptr, 0);
+    rowlen[r] = row_neighbours_any<NEN, MAXE>((int)r, n2e_ptr, n2e, ien, nEl, nen, nullptr, 0);
 }
 
 __global__ void k_slice_width(const int *__restrict__ rowlen, int64_t nN, int64_t nslices,
@@ -163,6 +202,7 @@ __global__ void k_slice_width(const int *__restrict__ rowlen, int64_t nN, int64_
     if (lane == 0) width[s] = w;
 }
 
+template <int NEN, int MAXE>
 __global__ void k_rowfill(const int64_t *__restrict__ n2e_ptr, const int *__restrict__ n2e,
                           const int *__restrict__ ien, int64_t nEl, int nen, int64_t nN,
                           const int *__restrict__ rowlen, const int64_t *__restrict__ sliceptr,
@@ -175,7 +215,7 @@ __global__ void k_rowfill(const int64_t *__restrict__ n2e_ptr, const int *__rest
     int64_t slab0 = sliceptr[s], width = sliceptr[s + 1] - slab0;
     int *base = col + slab0 * 32 + lane;
     int len = 0;
-    if (r < nN) len = row_neighbours((int)r, n2e_ptr, n2e, ien, nEl, nen, base, 32);
+    if (r < nN) len = row_neighbours_any<NEN, MAXE>((int)r, n2e_ptr, n2e, ien, nEl, nen, base, 32);
     int self = r < nN ? (int)r : 0;
     for (int64_t k = len; k < width; ++k) base[k * 32] = self;  // padding: (own node, value 0)
 }
@@ -419,7 +459,15 @@ extern "C" int sfem_pattern_build(sfem_ctx *ctx, sfem_mesh *m, int64_t *n_out, i
 
         // rows
         if ((st = sfem_dalloc(ctx, (void **)&m->rowlen, sizeof(int) * nN, "rowlen"))) break;
-        k_rowlen<<<blocks_for(nN, 128), 128, 0, s>>>(m->n2e_ptr, m->n2e, m->ien, nEl, nen, nN, m->rowlen);
+        // Q1 quads / hexes and Q2 quads: element node lists in registers
+        if (nen == 8)
+            k_rowlen<8, 8><<<blocks_for(nN, 128), 128, 0, s>>>(m->n2e_ptr, m->n2e, m->ien, nEl, nen, nN, m->rowlen);
+        else if (nen == 4)
+            k_rowlen<4, 6><<<blocks_for(nN, 128), 128, 0, s>>>(m->n2e_ptr, m->n2e, m->ien, nEl, nen, nN, m->rowlen);
+        else if (nen == 9)
+            k_rowlen<9, 4><<<blocks_for(nN, 128), 128, 0, s>>>(m->n2e_ptr, m->n2e, m->ien, nEl, nen, nN, m->rowlen);
+        else
+            k_rowlen<0, 0><<<blocks_for(nN, 128), 128, 0, s>>>(m->n2e_ptr, m->n2e, m->ien, nEl, nen, nN, m->rowlen);
         SFEM_LAUNCHED(ctx);
         m->nslices = sfem_cdiv(nN, 32);
         if ((st = sfem_dalloc(ctx, (void **)&widths, sizeof(int64_t) * m->nslices, "slice widths"))) break;
@@ -443,8 +491,12 @@ extern "C" int sfem_pattern_build(sfem_ctx *ctx, sfem_mesh *m, int64_t *n_out, i
             break;
         }
         if ((st = sfem_dalloc(ctx, (void **)&m->col, sizeof(int) * m->nslabs * 32, "pattern columns"))) break;
-        k_rowfill<<<blocks_for(m->nslices * 32, 128), 128, 0, s>>>(m->n2e_ptr, m->n2e, m->ien, nEl, nen, nN,
+        {
+            auto fill = nen == 8 ? k_rowfill<8, 8> : nen == 4 ? k_rowfill<4, 6> : nen == 9 ? k_rowfill<9, 4>
+                                                                                          : k_rowfill<0, 0>;
+            fill<<<blocks_for(m->nslices * 32, 128), 128, 0, s>>>(m->n2e_ptr, m->n2e, m->ien, nEl, nen, nN,
                                                                   m->rowlen, m->sliceptr, m->col);
+        }
         SFEM_LAUNCHED(ctx);
         st = sfem_check_device(ctx, "pattern build");
     } while (0);

@@ -890,7 +890,7 @@ __global__ void k_mg_csolve(const MgLevel C, int n, const float *cinv, const CgS
 // level (each of them bound by a few memory round trips, not by bytes).
 // The passes and their order are those of the grid-wide kernels.
 constexpr int MG_SOLO_T = 1024;
-constexpr int64_t MG_SOLO_MAX_NODES = 8192;  // largest level (and its finer neighbour / 8) run by the one CTA
+constexpr int64_t MG_SOLO_MAX_NODES = 1024;  // largest level (and its finer neighbour / 8) run by the one CTA
 template <int NDIM, int B>
 __global__ void __launch_bounds__(MG_SOLO_T)
 k_mg_solo(const sfem_dev::BatchArgs a, const BatchMesh M, const __grid_constant__ MgMesh mg, int solo,
