@@ -104,9 +104,10 @@ def parse_args(argv=None):
                     help="batch-leg solver arms (precision_precond)")
     ap.add_argument("--mixed-precond", default="both", choices=["both", "block_jacobi", "multigrid"],
                     help="preconditioners of the mixed leg (profiling runs pick one)")
-    ap.add_argument("--mg-delta", type=float, default=0.01,
+    ap.add_argument("--mg-delta", type=float, default=0.003,
                     help="reliable-update factor of the multigrid solves (mixed, batch, serve): multigrid drops "
-                         "the FP32 residual 10x in 2-3 iterations; 0.01 halves the FP64 refreshes at the same error")
+                         "the FP32 residual 10x in 2-3 iterations; 0.003 gives 4 FP64 refreshes at 128^3 (0.1: 10) at the same "
+                         "error")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (open loop)")
     ap.add_argument("--serve-requests", type=int, default=960, help="requests in the configured-rate stream")
     ap.add_argument("--serve-compare", type=int, default=64,
