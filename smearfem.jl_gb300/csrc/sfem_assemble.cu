@@ -172,7 +172,7 @@ k_element(const __grid_constant__ ElemTable tab, const double *__restrict__ X, c
 }
 
 template <int NEN, int B>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 k_gather(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const int *__restrict__ rowlen,
          const int64_t *__restrict__ n2e_ptr, const int *__restrict__ n2e, const int *__restrict__ ien,
          int64_t nEl, int64_t nN, int64_t nslices, const double *__restrict__ kbuf, double *__restrict__ val,
@@ -188,15 +188,19 @@ k_gather(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, cons
     const int64_t q0 = live ? n2e_ptr[r] : 0, q1 = live ? n2e_ptr[r + 1] : 0;
     GatherRow<NEN> R;
     R.load(n2e, q0, q1, ien, nEl, r);
+    // the next slot's column is loaded while this slot's blocks are
+    int cnext = width > 0 ? col[slab0 * 32 + lane] : 0;
     for (int64_t k = 0; k < width; ++k) {
         const int64_t slab = slab0 + k;
+        const int ccur = cnext;
+        if (k + 1 < width) cnext = col[(slab + 1) * 32 + lane];
         double acc[B * B];
 #pragma unroll
         for (int i = 0; i < B * B; ++i) acc[i] = 0.0;
         if (k < len && R.fast) {
-            R.template add<B>(col[slab * 32 + lane], kbuf, nEl, acc);
+            R.template add<B>(ccur, kbuf, nEl, acc);
         } else if (k < len) {
-            const int c = col[slab * 32 + lane];
+            const int c = ccur;
             int prev = -1;
             for (int64_t q = q0; q < q1; ++q) {
                 const int e = n2e[q];
