@@ -327,14 +327,17 @@ __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr,
         }
         if (own) {
             if constexpr (EPI == SPMV_Y) {
+                T rowdot = T(0);  // FP32: the row's share in FP32, one FP64 add per row
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
                     const int64_t d = r * B + i;
                     if constexpr (FUSE_P) pnew[d] = pd[i];
                     const T out = fx[i] ? T(0) : acc[i];
                     y[d] = out;
-                    dot += (double)pd[i] * (double)out;
+                    if constexpr (sizeof(T) == 4) rowdot = fma(pd[i], out, rowdot);
+                    else dot += (double)pd[i] * (double)out;
                 }
+                if constexpr (sizeof(T) == 4) dot += (double)rowdot;
             } else {
                 T res[B];
 #pragma unroll
@@ -343,14 +346,17 @@ __device__ __forceinline__ double grp_spmv(const int64_t *__restrict__ sliceptr,
 #pragma unroll
                     for (int i = 0; i < B; ++i) y[r * B + i] = res[i];
                 } else {
+                    T rowdot = T(0);
 #pragma unroll
                     for (int i = 0; i < B; ++i) {
                         T o = pd[i];
 #pragma unroll
                         for (int j = 0; j < B; ++j) o = fma(Mv[(r * B + i) * B + j], res[j], o);
                         y[r * B + i] = o;
-                        dot += (double)bv[r * B + i] * (double)o;
+                        if constexpr (sizeof(T) == 4) rowdot = fma(bv[r * B + i], o, rowdot);
+                        else dot += (double)bv[r * B + i] * (double)o;
                     }
+                    if constexpr (sizeof(T) == 4) dot += (double)rowdot;
                 }
             }
         }
@@ -425,11 +431,13 @@ __device__ __forceinline__ double2 cg_update(T *__restrict__ xv, T *__restrict__
             const int64_t node = nb + v * gstride;
             if (node < n1) {
                 T Xn[B], Z[B];
+                T nrr = T(0), nrz = T(0);  // FP32: the node's shares in FP32, one FP64 add each
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
                     Xn[i] = fma(alpha, P[v][i], X[v][i]);
                     R[v][i] = fma(-alpha, Q[v][i], R[v][i]);
-                    prr += (double)(R[v][i] * R[v][i]);
+                    if constexpr (sizeof(T) == 4) nrr = fma(R[v][i], R[v][i], nrr);
+                    else prr += (double)(R[v][i] * R[v][i]);
                 }
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
@@ -437,7 +445,12 @@ __device__ __forceinline__ double2 cg_update(T *__restrict__ xv, T *__restrict__
 #pragma unroll
                     for (int j = 0; j < B; ++j) zi = fma(Mi[v][i * B + j], R[v][j], zi);
                     Z[i] = zi;
-                    prz += (double)(R[v][i] * zi);
+                    if constexpr (sizeof(T) == 4) nrz = fma(R[v][i], zi, nrz);
+                    else prz += (double)(R[v][i] * zi);
+                }
+                if constexpr (sizeof(T) == 4) {
+                    prr += (double)nrr;
+                    prz += (double)nrz;
                 }
                 if constexpr (sizeof(T) == 4 && B == 2) {
                     *reinterpret_cast<float2 *>(xv + node * 2) = make_float2(Xn[0], Xn[1]);

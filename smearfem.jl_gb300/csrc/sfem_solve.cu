@@ -282,6 +282,7 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
         }
         if (r < nN) {
             if constexpr (EPI == sfem_dev::SPMV_Y) {
+                T rowdot = T(0);  // the row's share in T, one FP64 add per row (FP64 is a slow pipe on GB300)
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
                     const int64_t d = r * B + i;
@@ -292,12 +293,14 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
                         pd = fma(beta, pd, z[d]);
                         pout[d] = pd;
                     }
-                    if (MODE == 1) dot += (double)(pd * out);
+                    if (MODE == 1) rowdot = fma(pd, out, rowdot);
                 }
+                if (MODE == 1) dot += (double)rowdot;
             } else {
                 T res[B];
 #pragma unroll
                 for (int i = 0; i < B; ++i) res[i] = fixed[r * B + i] ? T(0) : bv[r * B + i] - acc[i];
+                T rowdot = T(0);
 #pragma unroll
                 for (int i = 0; i < B; ++i) {
                     T o = res[i];
@@ -305,10 +308,11 @@ k_spmv_sym(const int64_t *__restrict__ sptrU, const int *__restrict__ colU, cons
                         o = x[r * B + i];
 #pragma unroll
                         for (int j = 0; j < B; ++j) o = fma(Mv[(r * B + i) * B + j], res[j], o);
-                        dot += (double)bv[r * B + i] * (double)o;
+                        rowdot = fma(bv[r * B + i], o, rowdot);
                     }
                     y[r * B + i] = o;
                 }
+                if constexpr (EPI == sfem_dev::SPMV_SMOOTH) dot += (double)rowdot;
             }
         }
     }
@@ -403,6 +407,7 @@ k_update_node(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ 
         }
         V zv[B];
         T *ze = reinterpret_cast<T *>(zv);
+        T grz = T(0), grr = T(0);  // FP32: the group's shares in FP32, one FP64 add each
 #pragma unroll
         for (int n = 0; n < NPT; ++n)
 #pragma unroll
@@ -416,9 +421,18 @@ k_update_node(int64_t nN, T *__restrict__ x, T *__restrict__ r, T *__restrict__ 
                     for (int j = 0; j < B; ++j) zi = fma(me[(n * B + i) * B + j], re[n * B + j], zi);
                 }
                 ze[n * B + i] = zi;
-                rz += (double)(re[n * B + i] * zi);
-                rr += (double)(re[n * B + i] * re[n * B + i]);
+                if constexpr (sizeof(T) == 4) {
+                    grz = fma(re[n * B + i], zi, grz);
+                    grr = fma(re[n * B + i], re[n * B + i], grr);
+                } else {
+                    rz += (double)(re[n * B + i] * zi);
+                    rr += (double)(re[n * B + i] * re[n * B + i]);
+                }
             }
+        if constexpr (sizeof(T) == 4) {
+            rz += (double)grz;
+            rr += (double)grr;
+        }
         V *xd = reinterpret_cast<V *>(x + g * NPT * B);
         V *rd = reinterpret_cast<V *>(r + g * NPT * B);
         V *zd = reinterpret_cast<V *>(z + g * NPT * B);
