@@ -149,13 +149,18 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
             vp += 32 * B * B;
         }
         if (r < nN) {
+            T rowdot = T(0);  // FP32: the row's share in FP32, one FP64 add
 #pragma unroll
             for (int i = 0; i < B; ++i) {
                 const int64_t d = r * B + i;
                 const T out = fixed[d] ? T(0) : acc[i];
                 y[d] = out;
-                if (MODE == 1) dot += (double)(x[d] * out);
+                if (MODE == 1) {
+                    if constexpr (sizeof(T) == 4) rowdot = fma(x[d], out, rowdot);
+                    else dot += (double)(x[d] * out);
+                }
             }
+            if (MODE == 1 && sizeof(T) == 4) dot += (double)rowdot;
         }
     }
     if (MODE == 1) {
