@@ -140,14 +140,27 @@ k_element(const __grid_constant__ ElemTable tab, const double *__restrict__ X, c
             for (int i = 0; i < NDIM; ++i)
 #pragma unroll
                 for (int j = 0; j < NDIM; ++j) S[i][j] = 0.0;
+            if (a == bq) {  // symmetric: the upper triangle only (the pair is warp-uniform)
 #pragma unroll
-            for (int q = 0; q < NGP; ++q) {
-                const double *g = sG + ((int64_t)q * 32 + lane) * GS;
+                for (int q = 0; q < NGP; ++q) {
+                    const double *g = sG + ((int64_t)q * 32 + lane) * GS;
 #pragma unroll
-                for (int i = 0; i < NDIM; ++i) {
-                    const double wa = g[a * NDIM + i];
+                    for (int i = 0; i < NDIM; ++i) {
+                        const double wa = g[a * NDIM + i];
 #pragma unroll
-                    for (int j = 0; j < NDIM; ++j) S[i][j] = fma(wa, g[bq * NDIM + j], S[i][j]);
+                        for (int j = i; j < NDIM; ++j) S[i][j] = fma(wa, g[a * NDIM + j], S[i][j]);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < NGP; ++q) {
+                    const double *g = sG + ((int64_t)q * 32 + lane) * GS;
+#pragma unroll
+                    for (int i = 0; i < NDIM; ++i) {
+                        const double wa = g[a * NDIM + i];
+#pragma unroll
+                        for (int j = 0; j < NDIM; ++j) S[i][j] = fma(wa, g[bq * NDIM + j], S[i][j]);
+                    }
                 }
             }
             if (a == bq) {
