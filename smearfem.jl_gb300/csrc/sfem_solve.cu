@@ -112,7 +112,10 @@ __device__ bool reduce2_last(double a, double b, double *partial, unsigned int *
 }
 
 // y = mask .* (K x); MODE 1 additionally reduces x.y into pAp and sets alpha;
-// MODE 2 runs only while a mixed-precision refresh is pending.
+// MODE 2 runs only while a mixed-precision refresh is pending.  MODE 4 (the
+// Dirichlet lift K q_d, q_d zero but on the prescribed DOFs) skips the
+// blocks whose column entries of x are all zero: their terms are zeros, so
+// every sum is the same, and only rows next to prescribed DOFs read values.
 template <typename T, int B, int MODE>
 __global__ void __launch_bounds__(SPMV_T)
 k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const T *__restrict__ val, int64_t nN,
@@ -135,6 +138,16 @@ k_spmv(const int64_t *__restrict__ sliceptr, const int *__restrict__ col, const 
 #pragma unroll 2
         for (int64_t k = slab0; k < slab1; ++k) {
             const int c = __ldg(cp);
+            if constexpr (MODE == 4) {
+                bool nz = false;
+#pragma unroll
+                for (int j = 0; j < B; ++j) nz = nz || __ldg(&x[(int64_t)c * B + j]) != T(0);
+                if (!nz) {
+                    cp += 32;
+                    vp += 32 * B * B;
+                    continue;
+                }
+            }
             T v[B * B];
 #pragma unroll
             for (int i = 0; i < B * B; ++i) v[i] = __ldg(vp + i * 32);
@@ -788,11 +801,6 @@ __global__ void k_grid_check(const int *__restrict__ ien, int64_t nEl, int nen, 
     const int64_t gs = (int64_t)gridDim.x * blockDim.x;
 
 template <int NDIM, int B>
-__global__ void k_mg_fine(const sfem_dev::BatchArgs a, const BatchMesh M, const MgLevel F, const float *bj) {
-    SFEM_GRID_LOOP
-    sfem_dev::mg_pass_fine<NDIM, B>(a, M, F, bj, gt, gs);
-}
-template <int NDIM, int B>
 __global__ void k_mg_free(const sfem_dev::BatchArgs a, const BatchMesh M, const MgLevel F, const MgLevel C, int l) {
     SFEM_GRID_LOOP
     sfem_dev::mg_pass_free<NDIM, B>(a, M, F, C, l, gt, gs);
@@ -858,6 +866,51 @@ __global__ void k_mg_fine_stencil(const int64_t *__restrict__ sptrU, const int *
             for (int e = 0; e < B * B; ++e) F.A[sfem_dev::mg_a<NDIM, B>(r, st, e)] = 0.0f;
 #pragma unroll
     for (int c = 0; c < B; ++c) F.fr[r * B + c] = fixed[r * B + c] ? 0 : 1;
+}
+
+// Fine-level smoother W D^-1 (mg_pass_fine) from the fine stencil copy: the
+// same row sums in the same (ascending column) order, with fixed trip counts;
+// off-grid blocks are zero and add nothing.
+template <int NDIM, int B>
+__global__ void __launch_bounds__(256) k_mg_fine_st(const MgLevel F, const float *__restrict__ bj, float *minv) {
+    constexpr int S = NDIM == 2 ? 9 : 27;
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= F.nnode) return;
+    int ci[3];
+    sfem_dev::mg_coords<NDIM>(r, F.n, ci);
+    float Di[B * B];
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) Di[e] = bj[r * B * B + e];
+    float rs[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) rs[i] = 0.0f;
+#pragma unroll 3
+    for (int st = 0; st < S; ++st) {
+        int cj[3] = {0, 0, 0};
+        const int o[3] = {st % 3 - 1, (st / 3) % 3 - 1, NDIM == 3 ? st / 9 - 1 : 0};
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) cj[d] = min(max(ci[d] + o[d], 0), F.n);
+        const int64_t c = sfem_dev::mg_index<NDIM>(cj, F.n);
+        float blk[B * B];
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) blk[e] = F.A[sfem_dev::mg_a<NDIM, B>(r, st, e)];
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j) {
+                if (!F.fr[c * B + j]) continue;
+                float v = 0.0f;
+#pragma unroll
+                for (int mm = 0; mm < B; ++mm) v = fmaf(Di[i * B + mm], blk[mm * B + j], v);
+                rs[i] += fabsf(v);
+            }
+    }
+    float rho = 0.0f;
+#pragma unroll
+    for (int i = 0; i < B; ++i) rho = fmaxf(rho, rs[i]);
+    const float w = rho > 0.0f ? (4.0f / 3.0f) / rho : 0.0f;
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) minv[r * B * B + e] = w * Di[e];
 }
 
 // Galerkin product of the single-mesh set-up, one direction at a time.
@@ -1185,7 +1238,6 @@ int Solver::mg_build(const float *bj) {
     SFEM_TRY(sfem_copy_in(ctx, flag, &zero, sizeof(int), SFEM_MEM_HOST));
     auto grid = [&](int64_t work) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(sfem_cdiv(work, 256), 64 * ctx->num_sms)); };
     const int L = mg.nlev, S = NDIM == 2 ? 9 : 27;
-    k_mg_fine<NDIM, B><<<grid(mg.lev[0].nnode), 256, 0, ctx->stream>>>(mga, mgM, mg.lev[0], bj);
     // the fine level as a stencil level (scratch for this set-up): the
     // Galerkin pass then reads each fine block with one load group
     MgLevel F0 = mg.lev[0];
@@ -1205,6 +1257,8 @@ int Solver::mg_build(const float *bj) {
         F0.fr = (unsigned char *)scratch.p[1];
         k_mg_fine_stencil<NDIM, B><<<(unsigned)sfem_cdiv(m->nslices * 32, 256), 256, 0, ctx->stream>>>(
             K->sptrU, K->colU, K->valU, K->sptrL, K->lo, fixed, m->nslices, F0, flag);
+        // the fine smoother from the copy
+        k_mg_fine_st<NDIM, B><<<(unsigned)sfem_cdiv(nn, 256), 256, 0, ctx->stream>>>(F0, bj, mg.lev[0].minv);
         ctx->launches += 2;
     }
     // scratch of the direction-wise Galerkin passes, sized for level 0 -> 1
@@ -1251,7 +1305,6 @@ int Solver::mg_build(const float *bj) {
         }
     }
     k_mg_coarsest<NDIM, B><<<1, 512, 0, ctx->stream>>>(mg.lev[L - 1], mg.ndc, mg.cinv, mg.gj, flag);
-    SFEM_LAUNCHED(ctx);
     SFEM_LAUNCHED(ctx);
     int f = 0;
     SFEM_TRY(sfem_copy_out(ctx, &f, flag, sizeof(int), SFEM_MEM_HOST));
@@ -1638,9 +1691,14 @@ int Solver::run(const int64_t *fixed_dofs, int64_t nfix, const double *fixed_val
         SFEM_CUDA(ctx, cudaMemsetAsync(nofix, 0, nd, ctx->stream));
         unsigned char *keep = fixed;
         fixed = nofix;
-        if (b == 1) launch_spmv<double, 1>(K->val, ud, x64, false);
-        else if (b == 2) launch_spmv<double, 2>(K->val, ud, x64, false);
-        else launch_spmv<double, 3>(K->val, ud, x64, false);
+        auto lift = [&](auto kern) {
+            kern<<<spmv_grid, SPMV_T, 0, ctx->stream>>>(m->sliceptr, m->col, K->val, m->nN, m->nslices, ud, x64, fixed,
+                                                        S, partial);
+            SFEM_LAUNCHED(ctx);
+        };
+        if (b == 1) lift(k_spmv<double, 1, 4>);
+        else if (b == 2) lift(k_spmv<double, 2, 4>);
+        else lift(k_spmv<double, 3, 4>);
         fixed = keep;
         k_rhs<<<vec_grid, 256, 0, ctx->stream>>>(nd, fi, x64, fixed, bvec);
         SFEM_LAUNCHED(ctx);
