@@ -97,3 +97,17 @@ def test_served_multigrid_vs_oracle(sfem, oracle, coracle):
     u, res = outs[-1]
     assert res["status"] == 0 and res["iterations"] < 80, res
     assert _rel(u, _c_oracle(coracle, big)) <= TOL_U, res
+
+
+@pytest.mark.timeout(600)
+def test_single_mesh_multigrid_is_repeatable(sfem, ctx):
+    """The single-mesh hierarchy (fine stencil copy, direction-wise Galerkin
+    passes, one-CTA coarse levels) and the cycle use no value atomics: two
+    solves of the same problem return the same displacements bitwise, on an
+    odd-sized hex mesh and a quad mesh."""
+    for p in (sfem.meshgen.hex_problem(13, 91, jitter=0.2, e_sigma=0.5, nu=0.3, top="modes"),
+              sfem.meshgen.quad_problem(37, 5, jitter=0.15, nu=0.4, plane="strain", e_sigma=0.5, rtol=1e-10)):
+        u1, s1 = _single(sfem, ctx, p, "multigrid")
+        u2, s2 = _single(sfem, ctx, p, "multigrid")
+        assert s1["status"] == 0 and s1["iterations"] == s2["iterations"], (p.name, s1, s2)
+        assert np.array_equal(u1, u2), p.name
