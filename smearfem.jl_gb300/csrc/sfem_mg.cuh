@@ -15,8 +15,8 @@
 //
 // Coarse operators are Galerkin products A_{l+1} = P'^T A_l P' with A_0 the
 // masked K rounded to FP32.  Their node pattern is again the 3^ndim
-// neighbourhood, so they are stored as stencils: block (I, I + offset s) at
-// A[(s * B*B + e) * nnode + I], zero where the neighbour is off the grid.
+// neighbourhood, so they are stored as stencils: block (I, I + offset s) in
+// tiles of 32 nodes (mg_a), zero where the neighbour is off the grid.
 //
 // Cycle: V(1,1) with l1-scaled block Jacobi (x += w_i D_i^-1 r_i with
 // w_i = (4/3) / rho_i, rho_i = max row sum of |D_i^-1 A_i*|; convergent
