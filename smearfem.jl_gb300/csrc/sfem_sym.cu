@@ -55,11 +55,13 @@ __global__ void k_sym_width(const int *__restrict__ lenU, const int *__restrict_
 }
 
 // Upper part: columns (when colU != nullptr) and FP32 values from the FP64 K.
+// kdiag: each row's diagonal position (k_sym_len's lenL) when it is at hand,
+// else it is searched.
 template <int B>
 __global__ void k_sym_fill_upper(const int64_t *__restrict__ sliceptr, const int *__restrict__ col,
                                  const double *__restrict__ val, const int *__restrict__ rowlen, int64_t nN,
                                  int64_t nslices, const int64_t *__restrict__ sptrU, int *__restrict__ colU,
-                                 float *__restrict__ valU) {
+                                 float *__restrict__ valU, const int *__restrict__ kdiag) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t s = t >> 5;
     const int lane = (int)(t & 31);
@@ -67,7 +69,7 @@ __global__ void k_sym_fill_upper(const int64_t *__restrict__ sliceptr, const int
     const int64_t r = s * 32 + lane;
     const int64_t slab0 = sliceptr[s], u0 = sptrU[s], wU = sptrU[s + 1] - u0;
     const int len = r < nN ? rowlen[r] : 0;
-    const int kd = r < nN ? row_kdiag(col, slab0, lane, len, (int)r) : 0;
+    const int kd = r < nN ? (kdiag ? kdiag[r] : row_kdiag(col, slab0, lane, len, (int)r)) : 0;
     for (int64_t k = 0; k < wU; ++k) {
         const int64_t su = u0 + k;
         const bool live = k < len - kd;
@@ -83,22 +85,21 @@ template <int B>
 __global__ void k_sym_fill_lower(const int64_t *__restrict__ sliceptr, const int *__restrict__ col,
                                  const int *__restrict__ rowlen, int64_t nN, int64_t nslices,
                                  const int64_t *__restrict__ sptrU, const int64_t *__restrict__ sptrL,
-                                 int2 *__restrict__ lo, int *__restrict__ bad) {
+                                 int2 *__restrict__ lo, int *__restrict__ bad, const int *__restrict__ kdiag) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t s = t >> 5;
     const int lane = (int)(t & 31);
     if (s >= nslices) return;
     const int64_t r = s * 32 + lane;
     const int64_t slab0 = sliceptr[s], l0 = sptrL[s], wL = sptrL[s + 1] - l0;
-    const int len = r < nN ? rowlen[r] : 0;
-    const int kd = r < nN ? row_kdiag(col, slab0, lane, len, (int)r) : 0;
+    const int kd = r < nN ? kdiag[r] : 0;
     for (int64_t k = 0; k < wL; ++k) {
         int2 ent = make_int2(-1, 0);
         if (k < kd) {
             const int c = col[(slab0 + k) * 32 + lane];
             const int64_t cs0 = sliceptr[c >> 5];
             const int cl = c & 31, clen = rowlen[c];
-            const int ckd = row_kdiag(col, cs0, cl, clen, c);
+            const int ckd = kdiag[c];
             int lo_i = ckd, hi_i = clen - 1, pos = -1;  // r > c lies in c's upper part
             while (lo_i <= hi_i) {
                 const int mid = (lo_i + hi_i) >> 1;
@@ -122,11 +123,11 @@ __global__ void k_sym_fill_lower(const int64_t *__restrict__ sliceptr, const int
 }
 
 template <int B>
-void launch_fill_upper(sfem_ctx *ctx, const sfem_matrix *K, bool cols) {
+void launch_fill_upper(sfem_ctx *ctx, const sfem_matrix *K, bool cols, const int *kdiag = nullptr) {
     const sfem_mesh *m = K->mesh;
     const unsigned grid = (unsigned)sfem_cdiv(m->nslices * 32 > 0 ? m->nslices * 32 : 1, 128);
     k_sym_fill_upper<B><<<grid, 128, 0, ctx->stream>>>(m->sliceptr, m->col, K->val, m->rowlen, m->nN, m->nslices,
-                                                       K->sptrU, cols ? K->colU : nullptr, K->valU);
+                                                       K->sptrU, cols ? K->colU : nullptr, K->valU, kdiag);
     SFEM_LAUNCHED(ctx);
 }
 
@@ -193,20 +194,20 @@ int sfem_sym_build(sfem_ctx *ctx, sfem_matrix *K) {
         if ((st = sfem_dalloc(ctx, (void **)&K->valU, sizeof(float) * (K->nslabsU * 32 * b * b + 1), "sym values")))
             break;
         K->sym_state = 1;
-        if (b == 1) launch_fill_upper<1>(ctx, K, true);
-        else if (b == 2) launch_fill_upper<2>(ctx, K, true);
-        else launch_fill_upper<3>(ctx, K, true);
+        if (b == 1) launch_fill_upper<1>(ctx, K, true, lenL);
+        else if (b == 2) launch_fill_upper<2>(ctx, K, true, lenL);
+        else launch_fill_upper<3>(ctx, K, true, lenL);
         {
             const unsigned g = (unsigned)sfem_cdiv(nsl * 32 > 0 ? nsl * 32 : 1, 128);
             if (b == 1)
                 k_sym_fill_lower<1><<<g, 128, 0, ctx->stream>>>(m->sliceptr, m->col, m->rowlen, nN, nsl, K->sptrU,
-                                                               K->sptrL, K->lo, bad);
+                                                               K->sptrL, K->lo, bad, lenL);
             else if (b == 2)
                 k_sym_fill_lower<2><<<g, 128, 0, ctx->stream>>>(m->sliceptr, m->col, m->rowlen, nN, nsl, K->sptrU,
-                                                               K->sptrL, K->lo, bad);
+                                                               K->sptrL, K->lo, bad, lenL);
             else
                 k_sym_fill_lower<3><<<g, 128, 0, ctx->stream>>>(m->sliceptr, m->col, m->rowlen, nN, nsl, K->sptrU,
-                                                               K->sptrL, K->lo, bad);
+                                                               K->sptrL, K->lo, bad, lenL);
             SFEM_LAUNCHED(ctx);
         }
         int *hb = (int *)ctx->h_small;
