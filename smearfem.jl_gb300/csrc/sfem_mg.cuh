@@ -378,26 +378,74 @@ __device__ __forceinline__ void mg_pass_free(const BatchArgs &a, const BatchMesh
     }
 }
 
-// The pairs kx of one (kz, ky) row of the Galerkin sum on a stencil level,
-// NX of them (a fixed count, so that their loads are in flight together).
-template <int NDIM, int B, int NX>
-__device__ __forceinline__ void mg_galerkin_row(const MgLevel &F, const int (&pi)[3][7], const int (&pj)[3][7],
-                                                const float (&pw)[3][7], int ky, int kz, float *acc) {
+// Block (i, j) of the fine level (l = 0) from the per-mesh sliced-ELL K with
+// all its loads issued at once: the slab follows from the grid and is
+// clamped into the row's slice, so every load stays in bounds; the column
+// check afterwards says whether the pattern is the structured one.
+template <int NDIM, int B>
+__device__ __forceinline__ bool mg_block0(const BatchArgs &a, const BatchMesh &M, const MgLevel &L, const int ci[3],
+                                          const int cj[3], float *blk) {
+    int pos = 0, mul = 1;
+#pragma unroll
+    for (int d = 0; d < NDIM; ++d) {
+        const int lo = ci[d] > 0 ? 1 : 0;
+        pos += (cj[d] - ci[d] + lo) * mul;
+        mul *= 1 + lo + (ci[d] < L.n ? 1 : 0);
+    }
+    const int64_t r = M.node0 + mg_index<NDIM>(ci, L.n);
+    const int lane = (int)(r & 31);
+    const int64_t s0 = a.sliceptr[r >> 5], s1 = a.sliceptr[(r >> 5) + 1];
+    const bool inslice = s1 > s0;
+    const int64_t slab = min(s0 + pos, s1 - 1);
+    const int len = a.rowlen[r];
+    const int c = inslice ? a.col[slab * 32 + lane] : -1;
+    if (inslice) {
+        mg_fine_block<B>(a, slab, lane, blk);
+    } else {
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) blk[e] = 0.0f;
+    }
+    return pos < len && c == (int)(M.node0 + mg_index<NDIM>(cj, L.n));
+}
+
+// The pairs kx of one (kz, ky) row of the Galerkin sum, NX of them (a fixed
+// count, so that their loads are in flight together): on a stencil level
+// (L0 false) from the stencil, on the fine level of the per-mesh pipeline
+// (L0) from its K.
+template <int NDIM, int B, int NX, bool L0>
+__device__ __forceinline__ void mg_galerkin_row(const BatchArgs &a, const BatchMesh &M, const MgLevel &F,
+                                                const int (&pi)[3][7], const int (&pj)[3][7],
+                                                const float (&pw)[3][7], int ky, int kz, float *acc, int *flag) {
 #pragma unroll
     for (int kx = 0; kx < NX; ++kx) {
         const int ci[3] = {pi[0][kx], pi[1][ky], pi[2][kz]};
         const int cj[3] = {pj[0][kx], pj[1][ky], pj[2][kz]};
         const float w = pw[0][kx] * pw[1][ky] * pw[2][kz];
-        const int64_t li = mg_index<NDIM>(ci, F.n), lj = mg_index<NDIM>(cj, F.n);
-        const int st = mg_stencil<NDIM>(ci, cj);
         float blk[B * B];
+        bool fi[B], fj[B];
+        if constexpr (L0) {
+            if (!mg_block0<NDIM, B>(a, M, F, ci, cj, blk)) {
+                atomicMax(flag, (int)SFEM_BAD_INDEX);
+                continue;
+            }
+            mg_free<NDIM, B>(a, M, F, 0, ci, fi);
+            mg_free<NDIM, B>(a, M, F, 0, cj, fj);
+        } else {
+            const int64_t li = mg_index<NDIM>(ci, F.n), lj = mg_index<NDIM>(cj, F.n);
+            const int st = mg_stencil<NDIM>(ci, cj);
 #pragma unroll
-        for (int e = 0; e < B * B; ++e) blk[e] = F.A[mg_a<NDIM, B>(li, st, e)];
+            for (int e = 0; e < B * B; ++e) blk[e] = F.A[mg_a<NDIM, B>(li, st, e)];
+#pragma unroll
+            for (int c = 0; c < B; ++c) {
+                fi[c] = F.fr[li * B + c] != 0;
+                fj[c] = F.fr[lj * B + c] != 0;
+            }
+        }
 #pragma unroll
         for (int i = 0; i < B; ++i)
 #pragma unroll
             for (int j = 0; j < B; ++j)
-                if (F.fr[li * B + i] && F.fr[lj * B + j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
+                if (fi[i] && fj[j]) acc[i * B + j] = fmaf(w, blk[i * B + j], acc[i * B + j]);
     }
 }
 
@@ -451,7 +499,7 @@ __device__ __forceinline__ void mg_pass_galerkin(const BatchArgs &a, const Batch
                         ++k;
                     }
                 }
-                if (l >= 1) {
+                if (l >= 1 || !a.valU) {
                     const int npad = off[d] == 0 ? 7 : 3;
                     for (; k < npad; ++k) {
                         pi[d][k] = pj[d][k] = ccI;
@@ -463,8 +511,14 @@ __device__ __forceinline__ void mg_pass_galerkin(const BatchArgs &a, const Batch
             if (l >= 1) {
                 for (int kz = 0; kz < np[2]; ++kz)
                     for (int ky = 0; ky < np[1]; ++ky) {
-                        if (np[0] == 7) mg_galerkin_row<NDIM, B, 7>(F, pi, pj, pw, ky, kz, acc);
-                        else mg_galerkin_row<NDIM, B, 3>(F, pi, pj, pw, ky, kz, acc);
+                        if (np[0] == 7) mg_galerkin_row<NDIM, B, 7, false>(a, M, F, pi, pj, pw, ky, kz, acc, flag);
+                        else mg_galerkin_row<NDIM, B, 3, false>(a, M, F, pi, pj, pw, ky, kz, acc, flag);
+                    }
+            } else if (!a.valU) {
+                for (int kz = 0; kz < np[2]; ++kz)
+                    for (int ky = 0; ky < np[1]; ++ky) {
+                        if (np[0] == 7) mg_galerkin_row<NDIM, B, 7, true>(a, M, F, pi, pj, pw, ky, kz, acc, flag);
+                        else mg_galerkin_row<NDIM, B, 3, true>(a, M, F, pi, pj, pw, ky, kz, acc, flag);
                     }
             } else {
                 for (int kz = 0; kz < np[2]; ++kz)
